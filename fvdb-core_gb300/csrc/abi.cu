@@ -1,0 +1,28 @@
+// Library-wide C ABI helpers: version string and per-thread last CUDA error.
+#include <stdio.h>
+
+#include <atomic>
+
+#include "common.cuh"
+
+namespace fvgb {
+namespace {
+thread_local char g_last_error[256] = "";
+std::atomic<unsigned long long> g_launches{0};
+}
+
+void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+
+int record_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return FVGB_OK;
+    snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+    return FVGB_ECUDA;
+}
+
+}  // namespace fvgb
+
+extern "C" const char *fvgb_version(void) { return "fvdb_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" const char *fvgb_last_error(void) { return fvgb::g_last_error; }
+
+extern "C" uint64_t fvgb_launch_count(void) { return fvgb::g_launches.load(std::memory_order_relaxed); }

@@ -1,0 +1,265 @@
+// CUDA-core contractions: the plain FP32 form (no TF32) and the FP64 form.
+//
+// Forward:  y[m,:] (+)= sum_k x[map[m,k],:] . W[k]   (one CTA owns a 64x64 output tile; every
+//           output element is written exactly once, no atomics).  Offsets whose 64 map entries
+//           are all -1 are skipped.  With the transposed map and W^T strides the same kernel is
+//           the data gradient.
+// Wgrad:    dW[k,ci,co] = sum_m x[map[m,k],ci] * dy[m,co] with per-CTA partials and a
+//           fixed-order FP64 reduction across CTAs.
+//
+// Replaces the gather -> torch::mm_out -> scatter loop of
+// src/fvdb/detail/ops/convolution/backend/SparseConvolutionKernelMap.cu:116-415.
+#include "common.cuh"
+
+namespace fvgb {
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(NT) conv_fwd_simt_kernel(const T *__restrict__ x, int64_t n_x, int32_t cin,
+                                                           int64_t ldx, const int32_t *__restrict__ map,
+                                                           int64_t n_out, int32_t K, int64_t ldm,
+                                                           const T *__restrict__ w, int64_t wsk, int64_t wsci,
+                                                           int64_t wsco, T *__restrict__ y, int32_t cout,
+                                                           int64_t ldy, int32_t accumulate) {
+    __shared__ int32_t rows[BM];
+    __shared__ T As[BK][BM + 4];
+    __shared__ T Bs[BK][BN + 4];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int64_t m0 = (int64_t)blockIdx.x * BM;
+    const int32_t n0 = blockIdx.y * BN;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+
+    for (int32_t k = 0; k < K; ++k) {
+        int valid = 0;
+        if (tid < BM) {
+            const int64_t r = m0 + tid;
+            int32_t v = r < n_out ? map[r * ldm + k] : -1;
+            if (v >= n_x) v = -1;
+            rows[tid] = v;
+            valid = v >= 0;
+        }
+        if (!__syncthreads_or(valid)) continue;
+        for (int32_t c0 = 0; c0 < cin; c0 += BK) {
+#pragma unroll
+            for (int q = 0; q < (BM * BK) / NT; ++q) {
+                const int e = tid + q * NT, r = e / BK, c = e % BK;
+                const int32_t src = rows[r];
+                As[c][r] = (src >= 0 && c0 + c < cin) ? x[(int64_t)src * ldx + c0 + c] : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < (BK * BN) / NT; ++q) {
+                const int e = tid + q * NT, c = e / BN, n = e % BN;
+                Bs[c][n] = (c0 + c < cin && n0 + n < cout) ? w[k * wsk + (int64_t)(c0 + c) * wsci + (int64_t)(n0 + n) * wsco]
+                                                           : T(0);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int c = 0; c < BK; ++c) {
+                T a[4], bb[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) a[i] = As[c][ty * 4 + i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) bb[j] = Bs[c][tx * 4 + j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t r = m0 + ty * 4 + i;
+        if (r >= n_out) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int32_t n = n0 + tx * 4 + j;
+            if (n >= cout) continue;
+            T *dst = y + r * ldy + n;
+            *dst = accumulate ? (T)(*dst + acc[i][j]) : acc[i][j];
+        }
+    }
+}
+
+// Rows per wgrad chunk so that the grid has enough CTAs; deterministic in the sizes only.
+struct WgradPlan {
+    int64_t chunks, rows_per_chunk;
+    int32_t tiles_ci, tiles_co;
+};
+
+WgradPlan wgrad_plan(int64_t n_out, int32_t K, int32_t cin, int32_t cout) {
+    WgradPlan p;
+    p.tiles_ci = (int32_t)ceil_div(cin, BM);
+    p.tiles_co = (int32_t)ceil_div(cout, BN);
+    const int64_t per_chunk_ctas = (int64_t)K * p.tiles_ci * p.tiles_co;
+    int64_t chunks = ceil_div(2048, per_chunk_ctas);
+    const int64_t max_chunks = ceil_div(n_out > 0 ? n_out : 1, 256);
+    if (chunks > max_chunks) chunks = max_chunks;
+    if (chunks < 1) chunks = 1;
+    p.rows_per_chunk = ceil_div(ceil_div(n_out > 0 ? n_out : 1, chunks), BK) * BK;
+    p.chunks = ceil_div(n_out > 0 ? n_out : 1, p.rows_per_chunk);
+    return p;
+}
+
+template <typename T, typename AccT>
+__global__ void __launch_bounds__(NT) wgrad_simt_kernel(const T *__restrict__ x, int64_t n_x, int32_t cin,
+                                                        int64_t ldx, const int32_t *__restrict__ map,
+                                                        int64_t n_out, int32_t K, int64_t ldm,
+                                                        const T *__restrict__ dy, int32_t cout, int64_t lddy,
+                                                        int64_t rows_per_chunk, int32_t tiles_co,
+                                                        AccT *__restrict__ partials) {
+    __shared__ int32_t rows[BK];
+    __shared__ AccT Xs[BK][BM + 4];
+    __shared__ AccT Ds[BK][BN + 4];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int64_t chunk = blockIdx.x;
+    const int32_t k = blockIdx.y;
+    const int32_t ci0 = (blockIdx.z / tiles_co) * BM, co0 = (blockIdx.z % tiles_co) * BN;
+    const int64_t r_begin = chunk * rows_per_chunk;
+    int64_t r_end = r_begin + rows_per_chunk;
+    if (r_end > n_out) r_end = n_out;
+    AccT acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = AccT(0);
+    for (int64_t r0 = r_begin; r0 < r_end; r0 += BK) {
+        int valid = 0;
+        if (tid < BK) {
+            const int64_t r = r0 + tid;
+            int32_t v = r < r_end ? map[r * ldm + k] : -1;
+            if (v >= n_x) v = -1;
+            rows[tid] = v;
+            valid = v >= 0;
+        }
+        if (!__syncthreads_or(valid)) continue;
+#pragma unroll
+        for (int q = 0; q < (BK * BM) / NT; ++q) {
+            const int e = tid + q * NT, r = e / BM, c = e % BM;
+            const int32_t src = rows[r];
+            Xs[r][c] = (src >= 0 && ci0 + c < cin) ? (AccT)x[(int64_t)src * ldx + ci0 + c] : AccT(0);
+            Ds[r][c] = (src >= 0 && co0 + c < cout) ? (AccT)dy[(r0 + r) * lddy + co0 + c] : AccT(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < BK; ++r) {
+            AccT a[4], bb[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = Xs[r][ty * 4 + i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bb[j] = Ds[r][tx * 4 + j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    AccT *dst = partials + ((chunk * K + k) * (int64_t)cin) * cout;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int32_t ci = ci0 + ty * 4 + i;
+        if (ci >= cin) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int32_t co = co0 + tx * 4 + j;
+            if (co < cout) dst[(int64_t)ci * cout + co] = acc[i][j];
+        }
+    }
+}
+
+// dW[e] = sum over chunks (ascending) of partials[chunk][e], accumulated in FP64.
+template <typename AccT, typename OutT>
+__global__ void wgrad_reduce_kernel(const AccT *__restrict__ partials, int64_t chunks, int64_t per_chunk,
+                                    OutT *__restrict__ dw) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= per_chunk) return;
+    double s = 0.0;
+    for (int64_t c = 0; c < chunks; ++c) s += (double)partials[c * per_chunk + e];
+    dw[e] = (OutT)s;
+}
+
+}  // namespace
+}  // namespace fvgb
+
+using namespace fvgb;
+
+extern "C" int fvgb_conv_fwd_simt(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                  const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *w,
+                                  int64_t wsk, int64_t wsci, int64_t wsco, void *y, int32_t c_out, int64_t ldy,
+                                  int32_t accumulate, fvgb_stream_t stream) {
+    if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldm < K || ldx < c_in || ldy < c_out)
+        return FVGB_EINVAL;
+    if (n_out == 0) return FVGB_OK;
+    if (!map || !w || !y || (n_x > 0 && !x)) return FVGB_EINVAL;
+    const dim3 grid((unsigned)ceil_div(n_out, BM), (unsigned)ceil_div(c_out, BN));
+    if (grid.y > 65535) return FVGB_EINVAL;
+    cudaStream_t s = as_stream(stream);
+    if (dtype == FVGB_F32) {
+        conv_fwd_simt_kernel<float><<<grid, NT, 0, s>>>((const float *)x, n_x, c_in, ldx, map, n_out, K, ldm,
+                                                        (const float *)w, wsk, wsci, wsco, (float *)y, c_out, ldy,
+                                                        accumulate);
+    } else if (dtype == FVGB_F64) {
+        conv_fwd_simt_kernel<double><<<grid, NT, 0, s>>>((const double *)x, n_x, c_in, ldx, map, n_out, K, ldm,
+                                                         (const double *)w, wsk, wsci, wsco, (double *)y, c_out,
+                                                         ldy, accumulate);
+    } else {
+        return FVGB_ETYPE;
+    }
+    count_launches(1);
+    return launch_status();
+}
+
+extern "C" int fvgb_wgrad_workspace(int32_t dtype, int64_t n_out, int32_t K, int32_t c_in, int32_t c_out,
+                                    size_t *bytes) {
+    if (!bytes || K < 1 || c_in < 1 || c_out < 1 || n_out < 0) return FVGB_EINVAL;
+    const WgradPlan p = wgrad_plan(n_out, K, c_in, c_out);
+    const size_t elem = dtype == FVGB_F64 ? 8 : 4;
+    *bytes = (size_t)p.chunks * K * c_in * c_out * elem + 256;
+    return FVGB_OK;
+}
+
+extern "C" int fvgb_conv_wgrad_simt(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                    const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *dy,
+                                    int32_t c_out, int64_t lddy, void *dw, void *workspace,
+                                    size_t workspace_bytes, fvgb_stream_t stream) {
+    if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldm < K || ldx < c_in || lddy < c_out || !dw)
+        return FVGB_EINVAL;
+    size_t need = 0;
+    fvgb_wgrad_workspace(dtype, n_out, K, c_in, c_out, &need);
+    if (!workspace || workspace_bytes < need) return FVGB_ENOSPACE;
+    const WgradPlan p = wgrad_plan(n_out, K, c_in, c_out);
+    cudaStream_t s = as_stream(stream);
+    const int64_t per_chunk = (int64_t)K * c_in * c_out;
+    const dim3 grid((unsigned)p.chunks, (unsigned)K, (unsigned)(p.tiles_ci * p.tiles_co));
+    if (grid.y > 65535 || grid.z > 65535) return FVGB_EINVAL;
+    char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    if (dtype == FVGB_F32) {
+        float *part = reinterpret_cast<float *>(base);
+        if (n_out > 0)
+            wgrad_simt_kernel<float, float><<<grid, NT, 0, s>>>((const float *)x, n_x, c_in, ldx, map, n_out, K,
+                                                               ldm, (const float *)dy, c_out, lddy,
+                                                               p.rows_per_chunk, p.tiles_co, part);
+        wgrad_reduce_kernel<float, float><<<(unsigned)ceil_div(per_chunk, 256), 256, 0, s>>>(
+            part, n_out > 0 ? p.chunks : 0, per_chunk, (float *)dw);
+    } else if (dtype == FVGB_F64) {
+        double *part = reinterpret_cast<double *>(base);
+        if (n_out > 0)
+            wgrad_simt_kernel<double, double><<<grid, NT, 0, s>>>((const double *)x, n_x, c_in, ldx, map, n_out,
+                                                                 K, ldm, (const double *)dy, c_out, lddy,
+                                                                 p.rows_per_chunk, p.tiles_co, part);
+        wgrad_reduce_kernel<double, double><<<(unsigned)ceil_div(per_chunk, 256), 256, 0, s>>>(
+            part, n_out > 0 ? p.chunks : 0, per_chunk, (double *)dw);
+    } else {
+        return FVGB_ETYPE;
+    }
+    count_launches(n_out > 0 ? 2 : 1);
+    return launch_status();
+}

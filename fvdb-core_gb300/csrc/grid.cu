@@ -1,0 +1,393 @@
+// Device grid builder: jagged ijk -> sorted unique voxels in NanoVDB order -> leaf table
+// + leaf hash.  No host synchronisation inside any entry point; sizes that the caller
+// must allocate from (unique count, leaf count) are left in device memory.
+//
+// Reference behaviour replaced: dispatchCreateNanoGridFromIJK<kCUDA>
+// (src/fvdb/detail/ops/BuildGridFromIjk.cu:26-83), which loops over the grids on the
+// host and calls nanovdb::tools::cuda::voxelsToGrid per grid.
+#include <cub/cub.cuh>
+
+#include "common.cuh"
+
+namespace fvgb {
+namespace {
+
+struct SortWs {
+    uint64_t *keys_a, *keys_b;
+    int32_t *bidx_a, *bidx_b;
+    int32_t *flags;  // n+1
+    void *cub_tmp;
+    size_t cub_bytes;
+};
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+size_t cub_sort_bytes(int64_t n) {
+    size_t a = 0, b = 0, c = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, a, (uint64_t *)nullptr, (uint64_t *)nullptr,
+                                    (int32_t *)nullptr, (int32_t *)nullptr, n, 0, 63);
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (int32_t *)nullptr, (int32_t *)nullptr,
+                                    (uint64_t *)nullptr, (uint64_t *)nullptr, n, 0, 32);
+    cub::DeviceScan::ExclusiveSum(nullptr, c, (int32_t *)nullptr, (int32_t *)nullptr, n + 1);
+    size_t m = a > b ? a : b;
+    return m > c ? m : c;
+}
+
+size_t sort_ws_layout(int64_t n, SortWs *ws, char *base) {
+    size_t off = 0;
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    auto take = [&](size_t bytes) {
+        char *p = base ? base + off : nullptr;
+        off = align_up(off + bytes, 256);
+        return p;
+    };
+    SortWs w;
+    w.keys_a = (uint64_t *)take(nn * 8);
+    w.keys_b = (uint64_t *)take(nn * 8);
+    w.bidx_a = (int32_t *)take(nn * 4);
+    w.bidx_b = (int32_t *)take(nn * 4);
+    w.flags = (int32_t *)take((nn + 1) * 4);
+    w.cub_bytes = cub_sort_bytes(n);
+    w.cub_tmp = take(w.cub_bytes);
+    if (ws) *ws = w;
+    return off;
+}
+
+__global__ void keys_kernel(const int32_t *__restrict__ ijk, const int64_t *__restrict__ joff,
+                            int32_t B, int64_t n, uint64_t *__restrict__ keys,
+                            int32_t *__restrict__ bidx, int32_t *__restrict__ err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t x = ijk[3 * i], y = ijk[3 * i + 1], z = ijk[3 * i + 2];
+    if (!coord_in_range(x) || !coord_in_range(y) || !coord_in_range(z)) atomicExch(err, FVGB_ERANGE);
+    keys[i] = order_key(x, y, z);
+    bidx[i] = batch_of(joff, B, i);
+}
+
+__global__ void unique_flags_kernel(const uint64_t *__restrict__ keys,
+                                    const int32_t *__restrict__ bidx, int64_t n,
+                                    int32_t *__restrict__ flags) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    if (i == n) { flags[i] = 0; return; }
+    flags[i] = (i == 0 || keys[i] != keys[i - 1] || bidx[i] != bidx[i - 1]) ? 1 : 0;
+}
+
+__global__ void unique_write_kernel(const uint64_t *__restrict__ keys,
+                                    const int32_t *__restrict__ bidx,
+                                    const int32_t *__restrict__ pos, int64_t n,
+                                    int32_t *__restrict__ out_ijk) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool first = (i == 0 || keys[i] != keys[i - 1] || bidx[i] != bidx[i - 1]);
+    if (!first) return;
+    int32_t x, y, z;
+    key_to_coord(keys[i], x, y, z);
+    const int64_t p = pos[i];
+    out_ijk[3 * p] = x;
+    out_ijk[3 * p + 1] = y;
+    out_ijk[3 * p + 2] = z;
+}
+
+// out_joff[b] = number of unique voxels in grids < b  (bidx sorted ascending)
+__global__ void offsets_kernel(const int32_t *__restrict__ bidx, const int32_t *__restrict__ pos,
+                               int64_t n, int32_t B, int64_t *__restrict__ out_joff) {
+    const int32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > B) return;
+    int64_t lo = 0, hi = n;  // first i with bidx[i] >= b
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (bidx[mid] < b) lo = mid + 1; else hi = mid;
+    }
+    out_joff[b] = pos[lo];  // pos has n+1 entries; pos[n] = total
+}
+
+__global__ void leaf_flags_kernel(const int32_t *__restrict__ ijk, const int64_t *__restrict__ joff,
+                                  int32_t B, int64_t n, int32_t *__restrict__ flags) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t f = 1;
+    if (i > 0) {
+        const int32_t b0 = batch_of(joff, B, i - 1), b1 = batch_of(joff, B, i);
+        f = (b0 != b1 || (ijk[3 * i] >> 3) != (ijk[3 * i - 3] >> 3) ||
+             (ijk[3 * i + 1] >> 3) != (ijk[3 * i - 2] >> 3) ||
+             (ijk[3 * i + 2] >> 3) != (ijk[3 * i - 1] >> 3)) ? 1 : 0;
+    }
+    flags[i] = f;
+}
+
+__global__ void leaf_count_kernel(const int32_t *__restrict__ ids, int64_t n, int64_t *__restrict__ out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = n > 0 ? (int64_t)ids[n - 1] : 0;  // inclusive scan
+}
+
+__global__ void leaf_fill_kernel(const int32_t *__restrict__ ijk, const int64_t *__restrict__ joff,
+                                 int32_t B, int64_t n, const int32_t *__restrict__ leaf_ids,
+                                 FvgbLeaf *__restrict__ leaves) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t id = leaf_ids[i] - 1;  // inclusive scan
+    const int32_t x = ijk[3 * i], y = ijk[3 * i + 1], z = ijk[3 * i + 2];
+    FvgbLeaf &L = leaves[id];
+    const bool first = (i == 0) || leaf_ids[i - 1] != leaf_ids[i];
+    if (first) {
+        L.origin[0] = x & ~7;
+        L.origin[1] = y & ~7;
+        L.origin[2] = z & ~7;
+        L.batch = batch_of(joff, B, i);
+        L.base = i;
+    }
+    const uint32_t bit = leaf_bit(x, y, z);
+    atomicOr(reinterpret_cast<unsigned long long *>(&L.mask[bit >> 6]), 1ull << (bit & 63));
+}
+
+__global__ void leaf_finish_kernel(FvgbLeaf *__restrict__ leaves, int64_t L, int32_t *__restrict__ slots,
+                                   int64_t cap) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= L) return;
+    FvgbLeaf &lf = leaves[id];
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        lf.prefix[w] = (uint16_t)run;
+        run += __popcll(lf.mask[w]);
+    }
+    const uint64_t cap_mask = (uint64_t)cap - 1;
+    uint64_t h = leaf_hash(lf.batch, lf.origin[0] >> 3, lf.origin[1] >> 3, lf.origin[2] >> 3) & cap_mask;
+    for (int64_t probe = 0; probe < cap; ++probe) {
+        const int32_t prev = atomicCAS(slots + h, -1, (int32_t)id);
+        if (prev == -1) break;
+        h = (h + 1) & cap_mask;
+    }
+}
+
+__global__ void points_kernel(const float *__restrict__ pts, const int64_t *__restrict__ joff,
+                              int32_t B, int64_t n, const double *__restrict__ vs,
+                              const double *__restrict__ org, int32_t *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t b = batch_of(joff, B, i);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // VoxelCoordTransform(1/w, -o/w).apply(p).round() in the points' precision
+        // (src/fvdb/detail/VoxelCoordTransform.h:320-333, BuildGridFromPoints.cu:37-41)
+        const float inv = (float)(1.0 / vs[3 * b + a]);
+        const float tr = (float)(-org[3 * b + a] / vs[3 * b + a]);
+        const float v = pts[3 * i + a] * inv + tr;
+        out[3 * i + a] = (int32_t)floorf(v + 0.5f);
+    }
+}
+
+__global__ void conv_candidates_kernel(FvgbGrid g, int3 ks, int3 st, int coarse, int32_t kc,
+                                       int32_t *__restrict__ out, uint8_t *__restrict__ valid) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.num_voxels) return;
+    const int32_t x = g.ijk[3 * i], y = g.ijk[3 * i + 1], z = g.ijk[3 * i + 2];
+    if (coarse) {
+        // floor(ijk / stride) with the stride Coord applied x<->s0 (CoarseIjkForFineGrid.cu:34-35)
+        out[3 * i] = (int32_t)floor((double)x / st.x);
+        out[3 * i + 1] = (int32_t)floor((double)y / st.y);
+        out[3 * i + 2] = (int32_t)floor((double)z / st.z);
+        valid[i] = 1;
+        return;
+    }
+    const int lo0 = (ks.x % 2 == 0) ? 0 : -(ks.x - 1) / 2, hi0 = (ks.x % 2 == 0) ? ks.x - 1 : (ks.x - 1) / 2;
+    const int lo1 = (ks.y % 2 == 0) ? 0 : -(ks.y - 1) / 2, hi1 = (ks.y % 2 == 0) ? ks.y - 1 : (ks.y - 1) / 2;
+    const int lo2 = (ks.z % 2 == 0) ? 0 : -(ks.z - 1) / 2, hi2 = (ks.z % 2 == 0) ? ks.z - 1 : (ks.z - 1) / 2;
+    int64_t c = i * kc;
+    // BuildGridForConv.cu:99-121: di over k0 moves z, dk over k2 moves x; C remainder
+    for (int di = lo0; di <= hi0; ++di)
+        for (int dj = lo1; dj <= hi1; ++dj)
+            for (int dk = lo2; dk <= hi2; ++dk, ++c) {
+                const int32_t dx = x + dk, dy = y + dj, dz = z + di;
+                const bool ok = (dx % st.z == 0) && (dy % st.y == 0) && (dz % st.x == 0);
+                valid[c] = ok ? 1 : 0;
+                out[3 * c] = ok ? dx / st.z : 0;
+                out[3 * c + 1] = ok ? dy / st.y : 0;
+                out[3 * c + 2] = ok ? dz / st.x : 0;
+            }
+}
+
+__global__ void compact_flags_kernel(const uint8_t *__restrict__ valid, int64_t n, int32_t *__restrict__ f) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    f[i] = (i < n && valid[i]) ? 1 : 0;
+}
+
+__global__ void compact_write_kernel(const int32_t *__restrict__ ijk, const uint8_t *__restrict__ valid,
+                                     const int32_t *__restrict__ pos, int64_t n, int32_t *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !valid[i]) return;
+    const int64_t p = pos[i];
+    out[3 * p] = ijk[3 * i];
+    out[3 * p + 1] = ijk[3 * i + 1];
+    out[3 * p + 2] = ijk[3 * i + 2];
+}
+
+__global__ void compact_offsets_kernel(const int64_t *__restrict__ src_joff, int32_t B, int64_t per,
+                                       const int32_t *__restrict__ pos, int64_t *__restrict__ out) {
+    const int32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > B) return;
+    out[b] = pos[src_joff[b] * per];
+}
+
+constexpr int kThreads = 256;
+inline unsigned blocks_for(int64_t n) { return (unsigned)ceil_div(n > 0 ? n : 1, kThreads); }
+
+}  // namespace
+}  // namespace fvgb
+
+using namespace fvgb;
+
+extern "C" int fvgb_ijk_sort_unique_workspace(int64_t n, int32_t num_grids, size_t *bytes) {
+    if (!bytes || n < 0 || num_grids < 1) return FVGB_EINVAL;
+    *bytes = sort_ws_layout(n, nullptr, nullptr) + 256;
+    return FVGB_OK;
+}
+
+extern "C" int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids,
+                                    int64_t n, int32_t *out_ijk, int64_t *out_joffsets,
+                                    int32_t *err_dev, void *workspace, size_t workspace_bytes,
+                                    fvgb_stream_t stream) {
+    if (n < 0 || num_grids < 1 || !joffsets || !out_joffsets || !err_dev) return FVGB_EINVAL;
+    if (n > 0 && (!ijk || !out_ijk)) return FVGB_EINVAL;
+    if (n >= (int64_t)INT32_MAX) return FVGB_EINVAL;
+    cudaStream_t s = as_stream(stream);
+    char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    SortWs w;
+    const size_t need = sort_ws_layout(n, &w, base);
+    if (!workspace || need + 256 > workspace_bytes) return FVGB_ENOSPACE;
+    if (n == 0) {
+        if (cudaMemsetAsync(out_joffsets, 0, sizeof(int64_t) * (num_grids + 1), s) != cudaSuccess)
+            return launch_status();
+        return launch_status();
+    }
+    keys_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, joffsets, num_grids, n, w.keys_a, w.bidx_a, err_dev);
+    size_t tb = w.cub_bytes;
+    // 1) sort by voxel key (stable radix), 2) stable sort by grid index: grids stay
+    //    contiguous and every grid's voxels stay in key order.
+    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.bidx_a, w.bidx_b, n, 0, 63, s);
+    const uint64_t *keys = w.keys_b;
+    const int32_t *bidx = w.bidx_b;
+    if (num_grids > 1) {
+        int bits = 1;
+        while ((1ll << bits) < num_grids) ++bits;
+        tb = w.cub_bytes;
+        cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.bidx_b, w.bidx_a, w.keys_b, w.keys_a, n, 0, bits, s);
+        keys = w.keys_a;
+        bidx = w.bidx_a;
+    }
+    unique_flags_kernel<<<blocks_for(n + 1), kThreads, 0, s>>>(keys, bidx, n, w.flags);
+    tb = w.cub_bytes;
+    // exclusive scan in place over n+1 flags: pos[n] = unique count
+    int32_t *pos = reinterpret_cast<int32_t *>(w.keys_a == keys ? (void *)w.keys_b : (void *)w.keys_a);
+    cub::DeviceScan::ExclusiveSum(w.cub_tmp, tb, w.flags, pos, n + 1, s);
+    unique_write_kernel<<<blocks_for(n), kThreads, 0, s>>>(keys, bidx, pos, n, out_ijk);
+    offsets_kernel<<<(unsigned)ceil_div(num_grids + 1, kThreads), kThreads, 0, s>>>(bidx, pos, n, num_grids,
+                                                                                    out_joffsets);
+    count_launches(4);
+    return launch_status();
+}
+
+extern "C" int fvgb_scan_workspace(int64_t n, size_t *bytes) {
+    if (!bytes || n < 0) return FVGB_EINVAL;
+    size_t c = 0;
+    cub::DeviceScan::InclusiveSum(nullptr, c, (int32_t *)nullptr, (int32_t *)nullptr, n + 1);
+    size_t c2 = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, c2, (int32_t *)nullptr, (int32_t *)nullptr, n + 1);
+    if (c2 > c) c = c2;
+    *bytes = c + (size_t)(n + 2) * 4 + 512;
+    return FVGB_OK;
+}
+
+extern "C" int fvgb_grid_leaf_scan(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids,
+                                   int64_t n, int32_t *leaf_ids, int64_t *num_leaves_dev,
+                                   void *workspace, size_t workspace_bytes, fvgb_stream_t stream) {
+    if (n < 0 || num_grids < 1 || !num_leaves_dev || (n > 0 && (!ijk || !leaf_ids))) return FVGB_EINVAL;
+    size_t need = 0;
+    fvgb_scan_workspace(n, &need);
+    if (!workspace || workspace_bytes < need) return FVGB_ENOSPACE;
+    cudaStream_t s = as_stream(stream);
+    char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    int32_t *flags = reinterpret_cast<int32_t *>(base);
+    void *tmp = base + ((size_t)(n + 2) * 4 + 255) / 256 * 256;
+    size_t tb = need - ((size_t)(n + 2) * 4 + 255) / 256 * 256 - 256;
+    if (n > 0) {
+        leaf_flags_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, joffsets, num_grids, n, flags);
+        cub::DeviceScan::InclusiveSum(tmp, tb, flags, leaf_ids, n, s);
+    }
+    leaf_count_kernel<<<1, 32, 0, s>>>(leaf_ids, n, num_leaves_dev);
+    count_launches(n > 0 ? 2 : 1);
+    return launch_status();
+}
+
+extern "C" int fvgb_grid_index_build(const FvgbGrid *g, const int32_t *leaf_ids, fvgb_stream_t stream) {
+    if (!g || g->num_voxels < 0 || g->num_leaves < 0) return FVGB_EINVAL;
+    if (g->hash_capacity < 2 * g->num_leaves || (g->hash_capacity & (g->hash_capacity - 1)) != 0)
+        return FVGB_EINVAL;
+    cudaStream_t s = as_stream(stream);
+    FvgbLeaf *leaves = const_cast<FvgbLeaf *>(g->leaves);
+    int32_t *slots = const_cast<int32_t *>(g->hash_slots);
+    if (g->hash_capacity > 0 && cudaMemsetAsync(slots, 0xff, sizeof(int32_t) * g->hash_capacity, s) != cudaSuccess)
+        return launch_status();
+    if (g->num_leaves > 0 && cudaMemsetAsync(leaves, 0, sizeof(FvgbLeaf) * g->num_leaves, s) != cudaSuccess)
+        return launch_status();
+    if (g->num_voxels > 0) {
+        leaf_fill_kernel<<<blocks_for(g->num_voxels), kThreads, 0, s>>>(g->ijk, g->voxel_offsets, g->num_grids,
+                                                                       g->num_voxels, leaf_ids, leaves);
+        leaf_finish_kernel<<<blocks_for(g->num_leaves), kThreads, 0, s>>>(leaves, g->num_leaves, slots,
+                                                                         g->hash_capacity);
+        count_launches(2);
+    }
+    return launch_status();
+}
+
+extern "C" int fvgb_points_to_ijk(const float *points, const int64_t *joffsets, int32_t num_grids,
+                                  int64_t n, const double *voxel_sizes, const double *origins,
+                                  int32_t *out_ijk, fvgb_stream_t stream) {
+    if (n < 0 || num_grids < 1 || (n > 0 && (!points || !out_ijk || !voxel_sizes || !origins)))
+        return FVGB_EINVAL;
+    if (n == 0) return FVGB_OK;
+    points_kernel<<<blocks_for(n), kThreads, 0, as_stream(stream)>>>(points, joffsets, num_grids, n,
+                                                                     voxel_sizes, origins, out_ijk);
+    count_launches(1);
+    return launch_status();
+}
+
+extern "C" int fvgb_conv_grid_candidates(const FvgbGrid *g, const int32_t ksize[3], const int32_t stride[3],
+                                         int32_t *out_ijk, uint8_t *out_valid, fvgb_stream_t stream) {
+    if (!g || !ksize || !stride) return FVGB_EINVAL;
+    for (int a = 0; a < 3; ++a)
+        if (ksize[a] < 1 || stride[a] < 1) return FVGB_EINVAL;
+    if (g->num_voxels == 0) return FVGB_OK;
+    const int coarse = (stride[0] == 1 && stride[1] == 1 && stride[2] == 1) ||
+                       (stride[0] == ksize[0] && stride[1] == ksize[1] && stride[2] == ksize[2]);
+    const int32_t kc = coarse ? 1 : ksize[0] * ksize[1] * ksize[2];
+    conv_candidates_kernel<<<blocks_for(g->num_voxels), kThreads, 0, as_stream(stream)>>>(
+        *g, make_int3(ksize[0], ksize[1], ksize[2]), make_int3(stride[0], stride[1], stride[2]), coarse, kc,
+        out_ijk, out_valid);
+    count_launches(1);
+    return launch_status();
+}
+
+extern "C" int fvgb_compact_ijk(const int32_t *ijk, const uint8_t *valid, const int64_t *src_joffsets,
+                                int32_t num_grids, int64_t per_voxel, int64_t n, int32_t *out_ijk,
+                                int64_t *out_joffsets, void *workspace, size_t workspace_bytes,
+                                fvgb_stream_t stream) {
+    if (n < 0 || num_grids < 1 || per_voxel < 1 || !src_joffsets || !out_joffsets) return FVGB_EINVAL;
+    size_t need = 0;
+    fvgb_scan_workspace(n, &need);
+    if (!workspace || workspace_bytes < need) return FVGB_ENOSPACE;
+    cudaStream_t s = as_stream(stream);
+    char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    int32_t *flags = reinterpret_cast<int32_t *>(base);
+    const size_t head = ((size_t)(n + 2) * 4 + 255) / 256 * 256;
+    void *tmp = base + head;
+    size_t tb = need - head - 256;
+    compact_flags_kernel<<<blocks_for(n + 1), kThreads, 0, s>>>(valid, n, flags);
+    cub::DeviceScan::ExclusiveSum(tmp, tb, flags, flags, n + 1, s);  // in place: flags -> positions
+    compact_write_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, valid, flags, n, out_ijk);
+    compact_offsets_kernel<<<(unsigned)ceil_div(num_grids + 1, kThreads), kThreads, 0, s>>>(
+        src_joffsets, num_grids, per_voxel, flags, out_joffsets);
+    count_launches(3);
+    return launch_status();
+}

@@ -1,0 +1,574 @@
+// Host side of fvdb_gb300: the C++ PyTorch extension `fvdb._C`.
+//
+// It mirrors the reference's L2/L3 layers for the convolution path:
+//   GridImpl      <-> fvdb::detail::GridBatchImpl (src/fvdb/detail/GridBatchImpl.h)
+//   PackInfo      <-> fvdb::SparseConvPackInfo    (src/fvdb/SparseConvPackInfo.{h,cpp})
+//   conv_forward / conv_backward <-> the forward/backward bodies of
+//                     fvdb::detail::autograd::SparseConvolutionKernelMap / ImplicitGEMM
+//                     (src/fvdb/detail/autograd/SparseConvolution*.cpp); the autograd
+//                     Function itself is fvdb/_conv.py
+// Torch owns every buffer; all device work goes through the C ABI of libfvdb_gb300.so on the
+// current torch stream.  Errors map to ValueError / TypeError / RuntimeError exactly where the
+// reference uses TORCH_CHECK_VALUE / TORCH_CHECK_TYPE / TORCH_CHECK.
+#include <ATen/cuda/CUDAContext.h>
+#include <c10/cuda/CUDAGuard.h>
+#include <torch/extension.h>
+
+#include <optional>
+#include <string>
+#include <vector>
+
+#include "../../../include/fvdb_gb300.h"
+
+namespace fvgbh {
+
+using torch::Tensor;
+
+inline fvgb_stream_t cur_stream() { return (fvgb_stream_t)at::cuda::getCurrentCUDAStream().stream(); }
+
+void check_status(int st, const char *what) {
+    if (st == FVGB_OK) return;
+    std::string msg = std::string(what) + " failed";
+    if (st == FVGB_ECUDA) msg += std::string(": ") + fvgb_last_error();
+    switch (st) {
+        case FVGB_EINVAL: TORCH_CHECK_VALUE(false, msg, " (invalid argument)");
+        case FVGB_ERANGE: TORCH_CHECK_VALUE(false, msg, " (coordinate outside [-2^20, 2^20))");
+        case FVGB_ETYPE: TORCH_CHECK_TYPE(false, msg, " (unsupported dtype)");
+        case FVGB_ETIMEOUT: TORCH_CHECK(false, msg, " (device wait timed out)");
+        case FVGB_ENOSPACE: TORCH_CHECK(false, msg, " (workspace too small)");
+        default: TORCH_CHECK(false, msg);
+    }
+}
+
+Tensor workspace(size_t bytes, const torch::Device &dev) {
+    return torch::empty({(int64_t)std::max<size_t>(bytes, 256)}, torch::dtype(torch::kUInt8).device(dev));
+}
+
+int64_t next_pow2(int64_t v) {
+    int64_t p = 64;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+struct Vec3 {
+    int32_t v[3];
+};
+
+Vec3 to_vec3(const std::vector<int64_t> &x, const char *name) {
+    TORCH_CHECK_VALUE(x.size() == 3 || x.size() == 1, name, " must have 1 or 3 entries");
+    Vec3 r;
+    for (int a = 0; a < 3; ++a) r.v[a] = (int32_t)(x.size() == 1 ? x[0] : x[a]);
+    return r;
+}
+
+// ------------------------------------------------------------------------------------------
+struct GridImpl {
+    int64_t B = 0, N = 0, L = 0, cap = 0;
+    Tensor joffsets;       // int64 [B+1] device
+    Tensor joffsets_host;  // int64 [B+1] cpu
+    Tensor ijk;            // int32 [N,3] device
+    Tensor leaves;         // uint8 [L*128] device
+    Tensor hash;           // int32 [cap] device
+    Tensor voxel_sizes;    // float64 [B,3] cpu
+    Tensor origins;        // float64 [B,3] cpu
+    Tensor jidx_cache;
+
+    FvgbGrid view() const {
+        FvgbGrid g;
+        g.num_grids = (int32_t)B;
+        g.reserved = 0;
+        g.num_voxels = N;
+        g.num_leaves = L;
+        g.hash_capacity = cap;
+        g.voxel_offsets = joffsets.data_ptr<int64_t>();
+        g.ijk = N > 0 ? ijk.data_ptr<int32_t>() : nullptr;
+        g.leaves = L > 0 ? reinterpret_cast<const FvgbLeaf *>(leaves.data_ptr<uint8_t>()) : nullptr;
+        g.hash_slots = cap > 0 ? hash.data_ptr<int32_t>() : nullptr;
+        return g;
+    }
+    torch::Device device() const { return joffsets.device(); }
+};
+using GridPtr = std::shared_ptr<GridImpl>;
+
+Tensor per_grid_vec(const Tensor &t, int64_t B, const char *name) {
+    Tensor v = t.to(torch::kFloat64).cpu();
+    if (v.dim() == 0) v = v.reshape({1, 1}).expand({B, 3});
+    else if (v.dim() == 1) v = v.reshape({1, -1}).expand({B, 3});
+    TORCH_CHECK_VALUE(v.dim() == 2 && v.size(0) == B && v.size(1) == 3, name, " must broadcast to [", B, ", 3]");
+    return v.contiguous().clone();
+}
+
+// Sorted-unique voxels in index order + leaf table + hash (one host sync for the counts).
+GridPtr build_grid(const Tensor &ijk_in, const Tensor &joff_in, const Tensor &vs, const Tensor &org) {
+    TORCH_CHECK(ijk_in.is_cuda(), "fvdb_gb300 grids live on CUDA devices");
+    c10::cuda::CUDAGuard guard(ijk_in.device());
+    auto dev = ijk_in.device();
+    TORCH_CHECK_VALUE(ijk_in.dim() == 2 && ijk_in.size(1) == 3, "ijk must have shape (N, 3)");
+    TORCH_CHECK_TYPE(!ijk_in.is_floating_point(), "ijk must have an integer dtype");
+    Tensor ijk = ijk_in.to(torch::kInt32).contiguous();
+    Tensor joff = joff_in.to(dev, torch::kInt64).contiguous();
+    const int64_t B = joff.size(0) - 1;
+    TORCH_CHECK_VALUE(B >= 1, "a grid batch needs at least one grid");
+    const int64_t n = ijk.size(0);
+    auto g = std::make_shared<GridImpl>();
+    g->B = B;
+    g->voxel_sizes = per_grid_vec(vs, B, "voxel_sizes");
+    g->origins = per_grid_vec(org, B, "origins");
+    auto i32 = torch::dtype(torch::kInt32).device(dev);
+    Tensor out_ijk = torch::empty({std::max<int64_t>(n, 1), 3}, i32);
+    Tensor out_joff = torch::empty({B + 1}, torch::dtype(torch::kInt64).device(dev));
+    Tensor err = torch::zeros({1}, i32);
+    size_t wsb = 0;
+    check_status(fvgb_ijk_sort_unique_workspace(n, (int32_t)B, &wsb), "grid build (workspace)");
+    Tensor ws = workspace(wsb, dev);
+    auto s = cur_stream();
+    check_status(fvgb_ijk_sort_unique(n ? ijk.data_ptr<int32_t>() : nullptr, joff.data_ptr<int64_t>(), (int32_t)B,
+                                      n, out_ijk.data_ptr<int32_t>(), out_joff.data_ptr<int64_t>(),
+                                      err.data_ptr<int32_t>(), ws.data_ptr(), ws.numel(), s),
+                 "grid build (sort)");
+    Tensor host = torch::cat({out_joff, err.to(torch::kInt64)}).cpu();
+    TORCH_CHECK_VALUE(host[B + 1].item<int64_t>() == 0, "voxel coordinates must lie in [-2^20, 2^20)");
+    g->joffsets_host = host.narrow(0, 0, B + 1).contiguous();
+    g->joffsets = out_joff;
+    g->N = g->joffsets_host[B].item<int64_t>();
+    g->ijk = out_ijk.narrow(0, 0, g->N);
+    // leaves
+    Tensor leaf_ids = torch::empty({std::max<int64_t>(g->N, 1)}, i32);
+    Tensor nleaf = torch::zeros({1}, torch::dtype(torch::kInt64).device(dev));
+    size_t sb = 0;
+    check_status(fvgb_scan_workspace(g->N, &sb), "grid build (scan workspace)");
+    Tensor ws2 = workspace(sb, dev);
+    check_status(fvgb_grid_leaf_scan(g->N ? g->ijk.data_ptr<int32_t>() : nullptr, g->joffsets.data_ptr<int64_t>(),
+                                     (int32_t)B, g->N, leaf_ids.data_ptr<int32_t>(), nleaf.data_ptr<int64_t>(),
+                                     ws2.data_ptr(), ws2.numel(), s),
+                 "grid build (leaf scan)");
+    g->L = nleaf.item<int64_t>();
+    g->cap = next_pow2(2 * g->L);
+    g->leaves = torch::empty({std::max<int64_t>(g->L, 1) * (int64_t)sizeof(FvgbLeaf)}, torch::dtype(torch::kUInt8).device(dev));
+    g->hash = torch::empty({g->cap}, i32);
+    FvgbGrid v = g->view();
+    check_status(fvgb_grid_index_build(&v, leaf_ids.data_ptr<int32_t>(), s), "grid build (index)");
+    return g;
+}
+
+GridPtr grid_from_ijk(const Tensor &ijk, const Tensor &joffsets, const Tensor &vs, const Tensor &org) {
+    return build_grid(ijk, joffsets, vs, org);
+}
+
+GridPtr grid_from_points(const Tensor &points, const Tensor &joffsets, const Tensor &vs, const Tensor &org) {
+    TORCH_CHECK(points.is_cuda(), "fvdb_gb300 grids live on CUDA devices");
+    c10::cuda::CUDAGuard guard(points.device());
+    TORCH_CHECK_VALUE(points.dim() == 2 && points.size(1) == 3, "points must have shape (N, 3)");
+    TORCH_CHECK_TYPE(points.is_floating_point(), "points must have a floating point dtype");
+    const int64_t B = joffsets.size(0) - 1;
+    Tensor p = points.to(torch::kFloat32).contiguous();
+    Tensor joff = joffsets.to(points.device(), torch::kInt64).contiguous();
+    Tensor vsb = per_grid_vec(vs, B, "voxel_sizes"), orb = per_grid_vec(org, B, "origins");
+    Tensor vsd = vsb.to(points.device()), ord = orb.to(points.device());
+    Tensor ijk = torch::empty({p.size(0), 3}, torch::dtype(torch::kInt32).device(points.device()));
+    check_status(fvgb_points_to_ijk(p.data_ptr<float>(), joff.data_ptr<int64_t>(), (int32_t)B, p.size(0),
+                                    vsd.data_ptr<double>(), ord.data_ptr<double>(), ijk.data_ptr<int32_t>(),
+                                    cur_stream()),
+                 "points to ijk");
+    return build_grid(ijk, joff, vsb, orb);
+}
+
+// conv_grid: output voxel set of a (strided) convolution (BuildGridForConv.cu:181-255).
+GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, const std::vector<int64_t> &st_in) {
+    c10::cuda::CUDAGuard guard(g->device());
+    Vec3 ks = to_vec3(ks_in, "kernel_size"), st = to_vec3(st_in, "stride");
+    for (int a = 0; a < 3; ++a) {
+        TORCH_CHECK_VALUE(ks.v[a] > 0, "kernel_size must be positive");
+        TORCH_CHECK_VALUE(st.v[a] >= 0, "stride must be non-negative");
+    }
+    // stride 0 (the Python default) behaves as 1
+    for (int a = 0; a < 3; ++a)
+        if (st.v[a] == 0) st.v[a] = 1;
+    auto dev = g->device();
+    const bool coarse = (st.v[0] == 1 && st.v[1] == 1 && st.v[2] == 1) ||
+                        (st.v[0] == ks.v[0] && st.v[1] == ks.v[1] && st.v[2] == ks.v[2]);
+    const int64_t kc = coarse ? 1 : (int64_t)ks.v[0] * ks.v[1] * ks.v[2];
+    const int64_t n = g->N * kc;
+    auto i32 = torch::dtype(torch::kInt32).device(dev);
+    Tensor cand = torch::empty({std::max<int64_t>(n, 1), 3}, i32);
+    Tensor valid = torch::empty({std::max<int64_t>(n, 1)}, torch::dtype(torch::kUInt8).device(dev));
+    FvgbGrid v = g->view();
+    auto s = cur_stream();
+    check_status(fvgb_conv_grid_candidates(&v, ks.v, st.v, cand.data_ptr<int32_t>(), valid.data_ptr<uint8_t>(), s),
+                 "conv_grid (candidates)");
+    Tensor ijk, joff;
+    if (coarse) {
+        ijk = cand.narrow(0, 0, n);
+        joff = g->joffsets;
+    } else {
+        Tensor out = torch::empty({std::max<int64_t>(n, 1), 3}, i32);
+        joff = torch::empty({g->B + 1}, torch::dtype(torch::kInt64).device(dev));
+        size_t sb = 0;
+        check_status(fvgb_scan_workspace(n, &sb), "conv_grid (workspace)");
+        Tensor ws = workspace(sb, dev);
+        check_status(fvgb_compact_ijk(cand.data_ptr<int32_t>(), valid.data_ptr<uint8_t>(), g->joffsets.data_ptr<int64_t>(),
+                                      (int32_t)g->B, kc, n, out.data_ptr<int32_t>(), joff.data_ptr<int64_t>(),
+                                      ws.data_ptr(), ws.numel(), s),
+                     "conv_grid (compact)");
+        const int64_t m = joff[g->B].item<int64_t>();
+        ijk = out.narrow(0, 0, m);
+    }
+    return build_grid(ijk, joff, g->voxel_sizes, g->origins);
+}
+
+Tensor grid_jidx(const GridPtr &g) {
+    if (!g->jidx_cache.defined()) {
+        Tensor counts = (g->joffsets_host.narrow(0, 1, g->B) - g->joffsets_host.narrow(0, 0, g->B));
+        g->jidx_cache = torch::repeat_interleave(torch::arange(g->B, torch::kInt32), counts).to(g->device());
+    }
+    return g->jidx_cache;
+}
+
+// ------------------------------------------------------------------------------------------
+// Map tensors of one (kernel, stride, source, target) -- SparseConvPackInfo.
+struct PackInfo {
+    Vec3 ks, st;
+    GridPtr src, tgt;
+    int32_t K = 0;
+    std::optional<Tensor> out_in_map;      // [ceil(N_tgt/128)*128, K]
+    std::optional<Tensor> out_in_map_bwd;  // [ceil(N_src/128)*128, K]
+    std::optional<Tensor> nbmap, nbsizes;  // GS form
+    std::optional<Tensor> reorder_loc, sorted_mask, reorder_out_in_map, reduced_sorted_mask;
+    std::optional<Tensor> reorder_loc_bwd, reorder_out_in_map_bwd, sorted_mask_bwd_w, sorted_mask_bwd_d;
+    bool use_me = false, use_tf32 = false;
+    std::optional<bool> gs_use_me;
+    int64_t split_mask_num = 1;
+    bool training_built = false;
+};
+using PackPtr = std::shared_ptr<PackInfo>;
+
+PackPtr make_pack(const std::vector<int64_t> &ks_in, const std::vector<int64_t> &st_in, const GridPtr &src,
+                  const std::optional<GridPtr> &tgt) {
+    auto p = std::make_shared<PackInfo>();
+    p->ks = to_vec3(ks_in, "kernel_size");
+    p->st = to_vec3(st_in, "stride");
+    for (int a = 0; a < 3; ++a) {
+        TORCH_CHECK(p->ks.v[a] > 0, "Expect kernel size to be larger than {0,0,0}");
+        TORCH_CHECK(p->st.v[a] > 0, "Expect stride to be larger than 0");
+    }
+    const bool unit_stride = p->st.v[0] == 1 && p->st.v[1] == 1 && p->st.v[2] == 1;
+    const bool unit_kernel = p->ks.v[0] == 1 && p->ks.v[1] == 1 && p->ks.v[2] == 1;
+    p->src = src;
+    if (tgt.has_value()) p->tgt = *tgt;
+    else if (unit_stride) p->tgt = src;
+    else p->tgt = grid_conv_grid(src, ks_in, st_in);
+    TORCH_CHECK(p->src->device() == p->tgt->device(), "Source and target grids must both be on the same device");
+    TORCH_CHECK(!(unit_kernel && unit_stride), "1x1 conv does not need kernel map to be built!");
+    p->K = p->ks.v[0] * p->ks.v[1] * p->ks.v[2];
+    return p;
+}
+
+Tensor build_kmap(const GridPtr &src, const GridPtr &tgt, const Vec3 &ks, const Vec3 &st, int32_t K) {
+    c10::cuda::CUDAGuard guard(tgt->device());
+    TORCH_CHECK_VALUE(src->B == tgt->B, "source and target grids must have the same grid count");
+    const int64_t npad = (tgt->N + 127) / 128 * 128;
+    Tensor kmap = torch::empty({npad, K}, torch::dtype(torch::kInt32).device(tgt->device()));
+    if (npad > tgt->N) kmap.narrow(0, tgt->N, npad - tgt->N).fill_(-1);
+    FvgbGrid s = src->view(), t = tgt->view();
+    check_status(fvgb_kmap_build(&s, &t, ks.v, st.v, kmap.data_ptr<int32_t>(), K, nullptr, cur_stream()),
+                 "kernel map build");
+    return kmap;
+}
+
+const Tensor &pack_kmap(PackPtr p) {
+    if (!p->out_in_map) p->out_in_map = build_kmap(p->src, p->tgt, p->ks, p->st, p->K);
+    return *p->out_in_map;
+}
+
+const Tensor &pack_kmap_t(PackPtr p) {
+    if (!p->out_in_map_bwd) {
+        const Tensor &m = pack_kmap(p);
+        const int64_t npad = (p->src->N + 127) / 128 * 128;
+        Tensor t = torch::empty({npad, p->K}, m.options());
+        check_status(fvgb_kmap_transpose(m.data_ptr<int32_t>(), p->tgt->N, p->K, p->K, t.data_ptr<int32_t>(), npad,
+                                         p->K, cur_stream()),
+                     "kernel map transpose");
+        p->out_in_map_bwd = t;
+    }
+    return *p->out_in_map_bwd;
+}
+
+void pack_build_gather_scatter(PackPtr p, bool use_me) {
+    if (p->nbmap && p->nbsizes) {
+        TORCH_CHECK(p->gs_use_me.value_or(use_me) == use_me, "Gather scatter is already built with different use_me value");
+        return;
+    }
+    c10::cuda::CUDAGuard guard(p->tgt->device());
+    const Tensor &m = pack_kmap(p);
+    const int64_t n_out = p->tgt->N;
+    auto dev = m.device();
+    Tensor nboff = torch::empty({p->K + 1}, torch::dtype(torch::kInt64).device(dev));
+    size_t wsb = 0;
+    check_status(fvgb_nbmap_workspace(n_out, p->K, &wsb), "nbmap workspace");
+    Tensor ws = workspace(wsb, dev);
+    // the pair count is needed to size nbmap: count first, then write
+    Tensor counts = (m.narrow(0, 0, n_out) >= 0).sum(0, false, torch::kInt64);
+    const int64_t P = counts.sum().item<int64_t>();
+    Tensor nbmap = torch::empty({std::max<int64_t>(P, 1), 2}, torch::dtype(torch::kInt32).device(dev));
+    check_status(fvgb_nbmap_build(m.data_ptr<int32_t>(), n_out, p->K, p->K, nbmap.data_ptr<int32_t>(),
+                                  nboff.data_ptr<int64_t>(), ws.data_ptr(), ws.numel(), cur_stream()),
+                 "nbmap build");
+    p->nbmap = nbmap.narrow(0, 0, P);
+    p->nbsizes = counts.to(torch::kInt32);
+    p->gs_use_me = use_me;
+    p->use_me = use_me;
+}
+
+// Row masks, descending sort and tile-reduced masks for the sorted implicit-GEMM tensors
+// (SparseConvPackInfo.cpp:110-147); computed with torch ops for the drop-in properties.
+void sorted_tensors(const Tensor &map, int64_t n_valid, int64_t split, Tensor &sorted_mask, Tensor &reorder_loc,
+                    Tensor &reordered) {
+    const int64_t K = map.size(1), npad = map.size(0);
+    const int64_t len = (K + split - 1) / split;
+    std::vector<Tensor> masks;
+    Tensor valid = (map >= 0).to(torch::kInt32);
+    for (int64_t sidx = 0; sidx < split; ++sidx) {
+        const int64_t l = sidx == split - 1 ? K - sidx * len : len;
+        Tensor w = torch::pow(2, torch::arange(l, map.options().dtype(torch::kInt64))).to(torch::kInt32);
+        Tensor mk = (valid.narrow(1, sidx * len, l) * w).sum(1, false, torch::kInt32);
+        if (n_valid < npad) mk.narrow(0, n_valid, npad - n_valid).zero_();
+        masks.push_back(mk);
+    }
+    Tensor bitmask = torch::stack(masks, 0);
+    auto r = torch::sort(bitmask, -1, true);
+    sorted_mask = std::get<0>(r);
+    reorder_loc = std::get<1>(r).to(torch::kInt32);
+    std::vector<Tensor> cols;
+    for (int64_t k = 0; k < K; ++k) {
+        Tensor loc = reorder_loc[k / len].to(torch::kInt64);
+        cols.push_back(map.select(1, k).index_select(0, loc));
+    }
+    reordered = torch::stack(cols, 1).contiguous();
+}
+
+Tensor reduce_mask(const Tensor &sorted_mask, int64_t tile) {
+    const int64_t S = sorted_mask.size(0), n = sorted_mask.size(1);
+    const int64_t nt = (n + tile - 1) / tile;
+    Tensor padded = torch::zeros({S, nt * tile}, sorted_mask.options());
+    padded.narrow(1, 0, n).copy_(sorted_mask);
+    Tensor r = padded.view({S, nt, tile});
+    Tensor out = r.select(2, 0).clone();
+    for (int64_t i = 1; i < tile; ++i) out.bitwise_or_(r.select(2, i));
+    return out;
+}
+
+void pack_build_implicit_gemm(PackPtr p, bool sorted, int64_t split, bool training, int64_t split_bwd, bool tf32) {
+    if (p->reorder_loc && sorted)
+        TORCH_CHECK(p->reorder_loc->size(0) == split, "Implicit GEMM is already built with different splitMaskNum value");
+    c10::cuda::CUDAGuard guard(p->tgt->device());
+    const Tensor &m = pack_kmap(p);
+    p->use_tf32 = tf32;
+    p->split_mask_num = split;
+    if (sorted && !p->reorder_loc) {
+        Tensor sm, rl, ro;
+        sorted_tensors(m, p->tgt->N, split, sm, rl, ro);
+        p->sorted_mask = sm;
+        p->reorder_loc = rl;
+        p->reorder_out_in_map = ro;
+        p->reduced_sorted_mask = reduce_mask(sm, 128);
+    }
+    if (training && !p->training_built) {
+        const Tensor &mt = pack_kmap_t(p);
+        Tensor sm, rl, ro;
+        sorted_tensors(mt, p->src->N, split_bwd, sm, rl, ro);
+        p->reorder_loc_bwd = rl;
+        p->reorder_out_in_map_bwd = ro;
+        p->sorted_mask_bwd_w = reduce_mask(sm, 64);
+        p->sorted_mask_bwd_d = reduce_mask(sm, 128);
+        p->training_built = true;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Contractions.  W is viewed as [K, Cin, Cout] (any strides).
+int32_t fvgb_dtype(const Tensor &t) {
+    switch (t.scalar_type()) {
+        case torch::kFloat32: return FVGB_F32;
+        case torch::kFloat64: return FVGB_F64;
+        case torch::kBFloat16: return FVGB_BF16;
+        case torch::kFloat16: return FVGB_F16;
+        default: TORCH_CHECK_TYPE(false, "unsupported feature dtype ", t.scalar_type());
+    }
+    return -1;
+}
+
+// y[m] = sum_k x[map[m,k]] W[k]   for the first n_out rows of map
+Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &Wkio, bool transpose_w) {
+    c10::cuda::CUDAGuard guard(x.device());
+    const int64_t K = map.size(1);
+    const int64_t cin = transpose_w ? Wkio.size(2) : Wkio.size(1);
+    const int64_t cout = transpose_w ? Wkio.size(1) : Wkio.size(2);
+    TORCH_CHECK_VALUE(x.size(1) == cin, "channel mismatch");
+    Tensor y = torch::empty({n_out, cout}, x.options());
+    if (n_out == 0) return y;
+    Tensor w = Wkio.to(x.scalar_type());
+    const int64_t wsk = w.stride(0), wsci = transpose_w ? w.stride(2) : w.stride(1), wsco = transpose_w ? w.stride(1) : w.stride(2);
+    const int32_t dt = fvgb_dtype(x);
+    if (dt == FVGB_F32 || dt == FVGB_F64) {
+        check_status(fvgb_conv_fwd_simt(dt, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0), map.data_ptr<int32_t>(),
+                                        n_out, (int32_t)K, map.stride(0), w.data_ptr(), wsk, wsci, wsco, y.data_ptr(),
+                                        (int32_t)cout, y.stride(0), 0, cur_stream()),
+                     "sparse conv forward");
+    } else {
+        // 16-bit features on the CUDA-core form: FP32 accumulate, rounded once at the end.
+        Tensor xf = x.to(torch::kFloat32), wf = w.to(torch::kFloat32);
+        Tensor yf = torch::empty({n_out, cout}, xf.options());
+        check_status(fvgb_conv_fwd_simt(FVGB_F32, xf.data_ptr(), xf.size(0), (int32_t)cin, xf.stride(0),
+                                        map.data_ptr<int32_t>(), n_out, (int32_t)K, map.stride(0), wf.data_ptr(),
+                                        wf.stride(0), transpose_w ? wf.stride(2) : wf.stride(1),
+                                        transpose_w ? wf.stride(1) : wf.stride(2), yf.data_ptr(), (int32_t)cout,
+                                        yf.stride(0), 0, cur_stream()),
+                     "sparse conv forward");
+        y.copy_(yf);
+    }
+    return y;
+}
+
+// dW[k] = sum_m x[map[m,k]]^T dy[m]   -> [K, Cin, Cout]
+Tensor gather_wgrad(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &dy, int64_t K) {
+    c10::cuda::CUDAGuard guard(x.device());
+    const int64_t cin = x.size(1), cout = dy.size(1);
+    const bool wide = x.scalar_type() == torch::kFloat64;
+    Tensor xx = wide ? x : x.to(torch::kFloat32).contiguous();
+    Tensor dd = (wide ? dy : dy.to(torch::kFloat32)).contiguous();
+    const int32_t dt = wide ? FVGB_F64 : FVGB_F32;
+    Tensor dw = torch::empty({K, cin, cout}, xx.options());
+    size_t wsb = 0;
+    check_status(fvgb_wgrad_workspace(dt, n_out, (int32_t)K, (int32_t)cin, (int32_t)cout, &wsb), "wgrad workspace");
+    Tensor ws = workspace(wsb, x.device());
+    check_status(fvgb_conv_wgrad_simt(dt, xx.data_ptr(), xx.size(0), (int32_t)cin, xx.stride(0), map.data_ptr<int32_t>(),
+                                      n_out, (int32_t)K, map.stride(0), dd.data_ptr(), (int32_t)cout, dd.stride(0),
+                                      dw.data_ptr(), ws.data_ptr(), ws.numel(), cur_stream()),
+                 "sparse conv weight gradient");
+    return dw.to(x.scalar_type());
+}
+
+// ------------------------------------------------------------------------------------------
+// Forward / backward of one sparse convolution, called by the Python autograd Function.
+// Checks and permutes follow SparseConvolutionKernelMap.cpp:18-191.
+std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed) {
+    TORCH_CHECK_VALUE(x.is_contiguous(), "features must be contiguous");
+    TORCH_CHECK_TYPE(x.is_floating_point(), "features must have a floating point type");
+    TORCH_CHECK_VALUE(x.dim() == 2, "Expected features to have 2 dimensions (shape (n, nF)) but got ", x.dim(),
+                      " dimensions");
+    TORCH_CHECK_TYPE(weights.is_floating_point(), "kernels must have a floating point type");
+    for (int64_t i = 0; i < weights.dim(); ++i)
+        TORCH_CHECK_VALUE(weights.size(i) != 0, "kernels tensor has zero dimension (dim = ", i, ")");
+    TORCH_CHECK_VALUE(weights.dim() == 5, "Expected kernels to have 5 dimensions (shape (out_ch, in_ch, d, h, w)) but got ",
+                      weights.dim(), " dimensions");
+    TORCH_CHECK_VALUE(x.is_cuda() && weights.is_cuda(), "features and kernels must be CUDA tensors");
+    const int64_t n_src = p->src->N, n_tgt = p->tgt->N;
+    const int64_t K0 = weights.size(2), K1 = weights.size(3), K2 = weights.size(4);
+    TORCH_CHECK_VALUE(K0 == p->ks.v[0] && K1 == p->ks.v[1] && K2 == p->ks.v[2],
+                      "kernel spatial shape must match the kernel map's kernel_size");
+    int64_t cin, cout;
+    Tensor Wkio;
+    if (!transposed) {
+        TORCH_CHECK_VALUE(x.size(0) == n_src, "The number of input features must match the number of voxels");
+        TORCH_CHECK_VALUE(weights.size(1) == x.size(1), "Expected input channels of kernels (", weights.size(1),
+                          ") to equal input channels of features: ", x.size(1));
+        cout = weights.size(0);
+        cin = weights.size(1);
+        Wkio = weights.permute({4, 3, 2, 1, 0}).reshape({-1, cin, cout});
+    } else {
+        TORCH_CHECK_VALUE(x.size(0) == n_tgt, "The number of input features must match the number of voxels");
+        TORCH_CHECK_VALUE(weights.size(0) == x.size(1), "Expected input channels of kernels (", weights.size(0),
+                          ") to equal input channels of features: ", x.size(1));
+        cin = weights.size(0);
+        cout = weights.size(1);
+        Wkio = weights.permute({4, 3, 2, 0, 1}).reshape({-1, cin, cout});
+    }
+    Tensor y;
+    if (!transposed)
+        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false) : torch::empty({0, cout}, x.options());
+    else
+        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false) : torch::empty({0, cout}, x.options());
+    return {y, Wkio};
+}
+
+// Returns (dx, dW) with dW in the 5-D layout of the forward weights.
+std::vector<Tensor> conv_backward(const Tensor &dy_in, const Tensor &x, const Tensor &Wkio, PackPtr p, bool transposed,
+                                  bool need_dx, bool need_dw) {
+    Tensor dy = dy_in.contiguous();
+    const int64_t K = Wkio.size(0), cin = Wkio.size(1), cout = Wkio.size(2);
+    Tensor dx, dW;
+    if (!transposed) {
+        // dgrad: dx[i] = sum_k dy[mapT[i,k]] W[k]^T ;  wgrad: dW[k] = sum_m x[map[m,k]]^T dy[m]
+        if (need_dx) dx = gather_gemm(dy, pack_kmap_t(p), p->src->N, Wkio, true);
+        if (need_dw) dW = gather_wgrad(x, pack_kmap(p), p->tgt->N, dy, K);
+    } else {
+        if (need_dx) dx = gather_gemm(dy, pack_kmap(p), p->tgt->N, Wkio, true);
+        if (need_dw) dW = gather_wgrad(x, pack_kmap_t(p), p->src->N, dy, K);
+    }
+    if (need_dw) {
+        dW = dW.reshape({p->ks.v[2], p->ks.v[1], p->ks.v[0], cin, cout});
+        dW = transposed ? dW.permute({3, 4, 2, 1, 0}) : dW.permute({4, 3, 2, 1, 0});
+    }
+    return {dx, dW};
+}
+
+std::optional<Tensor> opt(const std::optional<Tensor> &t) { return t; }
+
+}  // namespace fvgbh
+
+PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
+    using namespace fvgbh;
+    namespace py = pybind11;
+    m.doc() = "fvdb_gb300 host extension: grids, kernel maps and sparse convolution on GB300";
+    m.def("version", []() { return std::string(fvgb_version()); });
+
+    py::class_<GridImpl, GridPtr>(m, "GridImpl")
+        .def_static("from_ijk", &grid_from_ijk, py::arg("ijk"), py::arg("joffsets"), py::arg("voxel_sizes"),
+                    py::arg("origins"))
+        .def_static("from_points", &grid_from_points, py::arg("points"), py::arg("joffsets"),
+                    py::arg("voxel_sizes"), py::arg("origins"))
+        .def("conv_grid", &grid_conv_grid)
+        .def_property_readonly("grid_count", [](const GridImpl &g) { return g.B; })
+        .def_property_readonly("total_voxels", [](const GridImpl &g) { return g.N; })
+        .def_property_readonly("total_leaf_nodes", [](const GridImpl &g) { return g.L; })
+        .def_property_readonly("ijk", [](const GridImpl &g) { return g.ijk; })
+        .def_property_readonly("joffsets", [](const GridImpl &g) { return g.joffsets; })
+        .def_property_readonly("joffsets_host", [](const GridImpl &g) { return g.joffsets_host; })
+        .def_property_readonly("voxel_sizes", [](const GridImpl &g) { return g.voxel_sizes; })
+        .def_property_readonly("origins", [](const GridImpl &g) { return g.origins; })
+        .def_property_readonly("leaves", [](const GridImpl &g) { return g.leaves; })
+        .def_property_readonly("hash", [](const GridImpl &g) { return g.hash; })
+        .def_property_readonly("device", [](const GridImpl &g) { return g.device(); })
+        .def("jidx", [](GridPtr g) { return grid_jidx(g); });
+
+    py::class_<PackInfo, PackPtr>(m, "PackInfoImpl")
+        .def(py::init([](std::vector<int64_t> k, std::vector<int64_t> s, GridPtr src, std::optional<GridPtr> tgt) {
+                 return make_pack(k, s, src, tgt);
+             }),
+             py::arg("kernel_size"), py::arg("stride"), py::arg("source_grid"), py::arg("target_grid") = py::none())
+        .def("kmap", [](PackPtr p) { return pack_kmap(p); })
+        .def("kmap_t", [](PackPtr p) { return pack_kmap_t(p); })
+        .def("build_gather_scatter", &pack_build_gather_scatter)
+        .def("build_implicit_gemm", &pack_build_implicit_gemm)
+        .def_property_readonly("kernel_size", [](const PackInfo &p) { return py::make_tuple(p.ks.v[0], p.ks.v[1], p.ks.v[2]); })
+        .def_property_readonly("stride", [](const PackInfo &p) { return py::make_tuple(p.st.v[0], p.st.v[1], p.st.v[2]); })
+        .def_property_readonly("source_grid", [](const PackInfo &p) { return p.src; })
+        .def_property_readonly("target_grid", [](const PackInfo &p) { return p.tgt; })
+        .def_property_readonly("out_in_map", [](const PackInfo &p) { return opt(p.out_in_map); })
+        .def_property_readonly("out_in_map_bwd", [](const PackInfo &p) { return opt(p.out_in_map_bwd); })
+        .def_property_readonly("neighborhood_map", [](const PackInfo &p) { return opt(p.nbmap); })
+        .def_property_readonly("neighborhood_sizes", [](const PackInfo &p) { return opt(p.nbsizes); })
+        .def_property_readonly("reorder_loc", [](const PackInfo &p) { return opt(p.reorder_loc); })
+        .def_property_readonly("sorted_mask", [](const PackInfo &p) { return opt(p.sorted_mask); })
+        .def_property_readonly("reorder_out_in_map", [](const PackInfo &p) { return opt(p.reorder_out_in_map); })
+        .def_property_readonly("reduced_sorted_mask", [](const PackInfo &p) { return opt(p.reduced_sorted_mask); })
+        .def_property_readonly("reorder_loc_bwd", [](const PackInfo &p) { return opt(p.reorder_loc_bwd); })
+        .def_property_readonly("reorder_out_in_map_bwd", [](const PackInfo &p) { return opt(p.reorder_out_in_map_bwd); })
+        .def_property_readonly("sorted_mask_bwd_w", [](const PackInfo &p) { return opt(p.sorted_mask_bwd_w); })
+        .def_property_readonly("sorted_mask_bwd_d", [](const PackInfo &p) { return opt(p.sorted_mask_bwd_d); })
+        .def_property_readonly("use_me", [](const PackInfo &p) { return p.use_me; })
+        .def_property_readonly("use_tf32", [](const PackInfo &p) { return p.use_tf32; });
+
+    m.def("conv_forward", &conv_forward);
+    m.def("conv_backward", &conv_backward);
+}

@@ -1,0 +1,304 @@
+// Kernel-map construction (integer hot path).
+//
+// Reference: dispatchConvolutionKernelMap<kCUDA>
+// (src/fvdb/detail/ops/convolution/pack_info/ConvolutionKernelMap.cu:14-58,104-138) runs one
+// thread per (leaf, voxel slot) -- inactive slots included -- and each active thread makes K
+// independent root-to-leaf NanoVDB accessor probes.
+//
+// Here one CTA owns one target leaf.  It stages the window of source leaves that the leaf's
+// kernel footprint can touch (masks, bases, per-word prefix counts) in shared memory with one
+// hash probe per source leaf, lists the leaf's active voxels, and then every thread produces
+// map entries (row r, offset k) with consecutive threads writing consecutive int32s of the
+// row-major [N_out, K] map: the only global traffic is the coalesced map write.
+#include <cub/cub.cuh>
+
+#include "common.cuh"
+
+namespace fvgb {
+namespace {
+
+constexpr int kKmapThreads = 256;
+constexpr int kMaxWindow = 216;  // 6x6x6 source leaves (e.g. k<=9, stride<=4)
+constexpr int kMaxKSmem = 1024;  // per-offset counters kept in shared memory
+
+struct KmapParams {
+    FvgbGrid src, tgt;
+    int32_t K0, K1, K2;     // user kernel size (k0 acts on ijk axis 2)
+    int32_t S0, S1, S2;     // user stride (s0 acts on ijk axis 2)
+    int32_t st0, st1, st2;  // floor(-k/2 + 1) per user component
+    int32_t K;
+    int64_t ld;
+    int32_t *kmap;
+    int32_t *nbsizes;
+};
+
+struct WinLeaf {
+    uint64_t mask[8];
+    int64_t base;  // -1: absent
+    uint32_t prefix[4];  // two uint16 per word
+};
+
+__device__ inline uint32_t win_prefix(const WinLeaf &w, uint32_t word) {
+    return (w.prefix[word >> 1] >> ((word & 1) * 16)) & 0xffffu;
+}
+
+__global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
+    __shared__ WinLeaf win[kMaxWindow];
+    __shared__ uint16_t slots[512];
+    __shared__ int32_t counts[kMaxKSmem];
+    __shared__ int32_t s_count;
+
+    const int64_t leaf_id = blockIdx.x;
+    const FvgbLeaf &tl = p.tgt.leaves[leaf_id];
+    const int32_t ox = tl.origin[0], oy = tl.origin[1], oz = tl.origin[2], b = tl.batch;
+    const int64_t tbase = tl.base;
+
+    // Source coordinate range of the footprint, per ijk axis.  Axis 0 (x) uses s2/k2, axis 2 (z) s0/k0.
+    const int32_t lo_x = ox * p.S2 + p.st2, hi_x = (ox + 7) * p.S2 + p.st2 + p.K2 - 1;
+    const int32_t lo_y = oy * p.S1 + p.st1, hi_y = (oy + 7) * p.S1 + p.st1 + p.K1 - 1;
+    const int32_t lo_z = oz * p.S0 + p.st0, hi_z = (oz + 7) * p.S0 + p.st0 + p.K0 - 1;
+    const int32_t lx0 = lo_x >> 3, ly0 = lo_y >> 3, lz0 = lo_z >> 3;
+    const int32_t wx = (hi_x >> 3) - lx0 + 1, wy = (hi_y >> 3) - ly0 + 1, wz = (hi_z >> 3) - lz0 + 1;
+    const int32_t W = wx * wy * wz;
+    const bool staged = W <= kMaxWindow;
+
+    if (threadIdx.x == 0) s_count = 0;
+    for (int k = threadIdx.x; k < p.K && k < kMaxKSmem; k += blockDim.x) counts[k] = 0;
+    if (staged) {
+        for (int w = threadIdx.x; w < W; w += blockDim.x) {
+            const int32_t ix = w / (wy * wz), iy = (w / wz) % wy, iz = w % wz;
+            const int32_t id = find_leaf(p.src, b, lx0 + ix, ly0 + iy, lz0 + iz);
+            WinLeaf &dst = win[w];
+            if (id < 0) {
+                dst.base = -1;
+                continue;
+            }
+            const FvgbLeaf &sl = p.src.leaves[id];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) dst.mask[q] = sl.mask[q];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                dst.prefix[q] = (uint32_t)sl.prefix[2 * q] | ((uint32_t)sl.prefix[2 * q + 1] << 16);
+            dst.base = sl.base;
+        }
+    }
+    // Active voxel slots of the target leaf, in index (bit) order.
+    for (int s = threadIdx.x; s < 512; s += blockDim.x) {
+        const uint64_t m = tl.mask[s >> 6];
+        if ((m >> (s & 63)) & 1ull) {
+            const uint32_t r = tl.prefix[s >> 6] + __popcll((s & 63) ? (m & ((1ull << (s & 63)) - 1ull)) : 0ull);
+            slots[r] = (uint16_t)s;
+            atomicAdd(&s_count, 1);
+        }
+    }
+    __syncthreads();
+
+    const int32_t cnt = s_count;
+    const int64_t total = (int64_t)cnt * p.K;
+    const int32_t K01 = p.K0 * p.K1;
+    for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+        const int32_t r = (int32_t)(e / p.K), k = (int32_t)(e - (int64_t)r * p.K);
+        const uint32_t s = slots[r];
+        const int32_t tx = ox + (int32_t)(s >> 6), ty = oy + (int32_t)((s >> 3) & 7), tz = oz + (int32_t)(s & 7);
+        // kIdx = (i2*K1 + i1)*K0 + i0 with i2 offsetting x (extent k2) and i0 offsetting z
+        const int32_t i2 = k / K01, i1 = (k / p.K0) % p.K1, i0 = k % p.K0;
+        const int32_t sx = tx * p.S2 + p.st2 + i2;
+        const int32_t sy = ty * p.S1 + p.st1 + i1;
+        const int32_t sz = tz * p.S0 + p.st0 + i0;
+        int64_t idx = -1;
+        if (staged) {
+            const int32_t w = (((sx >> 3) - lx0) * wy + ((sy >> 3) - ly0)) * wz + ((sz >> 3) - lz0);
+            const WinLeaf &wl = win[w];
+            if (wl.base >= 0) {
+                const uint32_t bit = leaf_bit(sx, sy, sz), word = bit >> 6;
+                const uint64_t m = wl.mask[word];
+                if ((m >> (bit & 63)) & 1ull)
+                    idx = wl.base + win_prefix(wl, word) +
+                          __popcll((bit & 63) ? (m & ((1ull << (bit & 63)) - 1ull)) : 0ull);
+            }
+        } else {
+            const int32_t id = find_leaf(p.src, b, sx >> 3, sy >> 3, sz >> 3);
+            if (id >= 0) idx = leaf_voxel_index(p.src.leaves[id], leaf_bit(sx, sy, sz));
+        }
+        p.kmap[(tbase + r) * p.ld + k] = (int32_t)idx;
+        if (p.nbsizes && idx >= 0) {
+            if (k < kMaxKSmem) atomicAdd(&counts[k], 1);
+            else atomicAdd(p.nbsizes + k, 1);
+        }
+    }
+    if (p.nbsizes) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < p.K && k < kMaxKSmem; k += blockDim.x)
+            if (counts[k]) atomicAdd(p.nbsizes + k, counts[k]);
+    }
+}
+
+__global__ void fill_kernel(int32_t *__restrict__ p, int64_t n, int32_t v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+__global__ void transpose_kernel(const int32_t *__restrict__ kmap, int64_t n_out, int32_t K, int64_t ld,
+                                 int32_t *__restrict__ mapT, int64_t n_in, int64_t ldT) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_out * K) return;
+    const int64_t o = e / K;
+    const int32_t k = (int32_t)(e - o * K);
+    const int32_t i = kmap[o * ld + k];
+    if (i >= 0 && i < n_in) mapT[(int64_t)i * ldT + k] = (int32_t)o;
+}
+
+// ---- gather-scatter neighbour map (per offset, ordered by output row) --------------------
+constexpr int kNbRows = 256;
+
+// counts[k * nblk + blk] = valid entries of column k in rows [blk*256, blk*256+256)
+__global__ void __launch_bounds__(256) nb_count_kernel(const int32_t *__restrict__ kmap, int64_t n_out,
+                                                       int32_t K, int64_t ld, int64_t nblk,
+                                                       int32_t *__restrict__ counts) {
+    const int64_t blk = blockIdx.x;
+    const int64_t r0 = blk * kNbRows;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = warp; k < K; k += blockDim.x / 32) {
+        int c = 0;
+        for (int r = lane; r < kNbRows; r += 32) {
+            const int64_t row = r0 + r;
+            if (row < n_out && kmap[row * ld + k] >= 0) ++c;
+        }
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) counts[(int64_t)k * nblk + blk] = c;
+    }
+}
+
+__global__ void __launch_bounds__(256) nb_write_kernel(const int32_t *__restrict__ kmap, int64_t n_out,
+                                                       int32_t K, int64_t ld, int64_t nblk,
+                                                       const int32_t *__restrict__ offs,
+                                                       int32_t *__restrict__ nbmap) {
+    const int64_t blk = blockIdx.x;
+    const int64_t r0 = blk * kNbRows;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = warp; k < K; k += blockDim.x / 32) {
+        int64_t base = offs[(int64_t)k * nblk + blk];
+        for (int r = lane; r < kNbRows; r += 32) {
+            const int64_t row = r0 + r;
+            const int32_t v = row < n_out ? kmap[row * ld + k] : -1;
+            const unsigned bal = __ballot_sync(0xffffffffu, v >= 0);
+            if (v >= 0) {
+                const int64_t pos = base + __popc(bal & ((1u << lane) - 1u));
+                nbmap[2 * pos] = v;
+                nbmap[2 * pos + 1] = (int32_t)row;
+            }
+            base += __popc(bal);
+        }
+    }
+}
+
+__global__ void nb_offsets_kernel(const int32_t *__restrict__ offs, int32_t K, int64_t nblk,
+                                  int64_t *__restrict__ nboffsets) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > K) return;
+    nboffsets[k] = offs[(int64_t)k * nblk];  // offs has K*nblk + 1 entries (exclusive scan)
+}
+
+__global__ void masks_kernel(const int32_t *__restrict__ kmap, int64_t n_out, int32_t K, int64_t ld,
+                             uint32_t *__restrict__ row_mask, uint32_t *__restrict__ tile_mask) {
+    __shared__ uint32_t wm[4];
+    const int64_t row = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    uint32_t m = 0;
+    if (row < n_out)
+        for (int k = 0; k < K; ++k) m |= (kmap[row * ld + k] >= 0 ? 1u : 0u) << k;
+    if (row_mask && row < n_out) row_mask[row] = m;
+    for (int o = 16; o > 0; o >>= 1) m |= __shfl_xor_sync(0xffffffffu, m, o);
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0 && tile_mask) tile_mask[blockIdx.x] = wm[0] | wm[1] | wm[2] | wm[3];
+}
+
+}  // namespace
+}  // namespace fvgb
+
+using namespace fvgb;
+
+extern "C" int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const int32_t ksize[3],
+                               const int32_t stride[3], int32_t *kmap, int64_t ld, int32_t *nbsizes,
+                               fvgb_stream_t stream) {
+    if (!src || !tgt || !ksize || !stride) return FVGB_EINVAL;
+    for (int a = 0; a < 3; ++a)
+        if (ksize[a] < 1 || stride[a] < 1) return FVGB_EINVAL;
+    if (src->num_grids != tgt->num_grids) return FVGB_EINVAL;
+    const int64_t K = (int64_t)ksize[0] * ksize[1] * ksize[2];
+    if (K > (1 << 20) || ld < K) return FVGB_EINVAL;
+    if (tgt->num_voxels == 0 || tgt->num_leaves == 0) return FVGB_OK;
+    if (!kmap) return FVGB_EINVAL;
+    KmapParams p;
+    p.src = *src;
+    p.tgt = *tgt;
+    p.K0 = ksize[0]; p.K1 = ksize[1]; p.K2 = ksize[2];
+    p.S0 = stride[0]; p.S1 = stride[1]; p.S2 = stride[2];
+    // kernelStart = floor(-K/2 + 1) (ConvolutionKernelMap.cu:114-116)
+    p.st0 = (int32_t)floor(-ksize[0] / 2.0 + 1.0);
+    p.st1 = (int32_t)floor(-ksize[1] / 2.0 + 1.0);
+    p.st2 = (int32_t)floor(-ksize[2] / 2.0 + 1.0);
+    p.K = (int32_t)K;
+    p.ld = ld;
+    p.kmap = kmap;
+    p.nbsizes = nbsizes;
+    if (tgt->num_leaves > INT32_MAX) return FVGB_EINVAL;
+    kmap_leaf_kernel<<<(unsigned)tgt->num_leaves, kKmapThreads, 0, as_stream(stream)>>>(p);
+    count_launches(1);
+    return launch_status();
+}
+
+extern "C" int fvgb_kmap_transpose(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, int32_t *mapT,
+                                   int64_t n_in, int64_t ldT, fvgb_stream_t stream) {
+    if (K < 1 || ld < K || ldT < K || n_out < 0 || n_in < 0) return FVGB_EINVAL;
+    cudaStream_t s = as_stream(stream);
+    if (n_in > 0) fill_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n_in * ldT, 256), 65535 * 8), 256, 0, s>>>(mapT, n_in * ldT, -1);
+    if (n_out > 0)
+        transpose_kernel<<<(unsigned)ceil_div(n_out * K, 256), 256, 0, s>>>(kmap, n_out, K, ld, mapT, n_in, ldT);
+    count_launches((n_in > 0) + (n_out > 0));
+    return launch_status();
+}
+
+extern "C" int fvgb_nbmap_workspace(int64_t n_out, int32_t K, size_t *bytes) {
+    if (!bytes || n_out < 0 || K < 1) return FVGB_EINVAL;
+    const int64_t nblk = ceil_div(n_out > 0 ? n_out : 1, kNbRows);
+    const int64_t m = nblk * K + 1;
+    size_t c = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, c, (int32_t *)nullptr, (int32_t *)nullptr, m);
+    *bytes = c + (size_t)m * 4 * 2 + 1024;
+    return FVGB_OK;
+}
+
+extern "C" int fvgb_nbmap_build(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, int32_t *nbmap,
+                                int64_t *nboffsets, void *workspace, size_t workspace_bytes,
+                                fvgb_stream_t stream) {
+    if (K < 1 || ld < K || n_out < 0 || !nboffsets) return FVGB_EINVAL;
+    size_t need = 0;
+    fvgb_nbmap_workspace(n_out, K, &need);
+    if (!workspace || workspace_bytes < need) return FVGB_ENOSPACE;
+    cudaStream_t s = as_stream(stream);
+    const int64_t nblk = ceil_div(n_out > 0 ? n_out : 1, kNbRows);
+    const int64_t m = nblk * K + 1;
+    char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    int32_t *counts = reinterpret_cast<int32_t *>(base);
+    int32_t *offs = counts + ((m + 63) / 64 * 64);
+    void *tmp = offs + ((m + 63) / 64 * 64);
+    size_t tb = need - 1024 - (size_t)m * 8;
+    cudaMemsetAsync(counts, 0, sizeof(int32_t) * m, s);
+    if (n_out > 0) nb_count_kernel<<<(unsigned)nblk, 256, 0, s>>>(kmap, n_out, K, ld, nblk, counts);
+    cub::DeviceScan::ExclusiveSum(tmp, tb, counts, offs, m, s);
+    if (n_out > 0) nb_write_kernel<<<(unsigned)nblk, 256, 0, s>>>(kmap, n_out, K, ld, nblk, offs, nbmap);
+    nb_offsets_kernel<<<(unsigned)ceil_div(K + 1, 128), 128, 0, s>>>(offs, K, nblk, nboffsets);
+    count_launches(n_out > 0 ? 3 : 1);
+    return launch_status();
+}
+
+extern "C" int fvgb_kmap_masks(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, uint32_t *row_mask,
+                               uint32_t *tile_mask, fvgb_stream_t stream) {
+    if (K < 1 || K > 32 || ld < K || n_out < 0) return FVGB_EINVAL;
+    if (n_out == 0) return FVGB_OK;
+    masks_kernel<<<(unsigned)ceil_div(n_out, 128), 128, 0, as_stream(stream)>>>(kmap, n_out, K, ld, row_mask,
+                                                                               tile_mask);
+    count_launches(1);
+    return launch_status();
+}

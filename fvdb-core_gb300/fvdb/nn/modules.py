@@ -1,0 +1,119 @@
+"""fvdb.nn.SparseConv3d on the GB300 kernels (reference: fvdb/nn/modules.py:156-404).
+
+The module keeps the reference's constructor, weight layout ((Do, Di, K0, K1, K2) with
+(K2, K1, K0, Di, Do) memory), initialisation, kernel-map caching through VDBTensor, 1x1x1
+shortcut and bias.  ``backend`` and ``allow_tf32`` stay as accepted class attributes; every
+value runs the same implementation.  ``precision`` selects the arithmetic of the
+contraction for floating-point features: "native" (the features' dtype), "bf16" or "fp8"
+(E4M3 with per-channel scales); accumulation is always FP32 or wider.
+"""
+
+from __future__ import annotations
+
+import math
+from typing import Optional, Sequence, Union
+
+import torch
+import torch.nn as nn
+
+from ..grid_batch import GridBatch
+from ..sparse_conv_pack_info import ConvPackBackend, SparseConvPackInfo
+from .vdbtensor import VDBTensor
+
+
+class SparseConv3d(nn.Module):
+    backend: str = "default"
+    allow_tf32: bool = True
+    precision: str = "native"
+
+    def __init__(
+        self,
+        in_channels: int,
+        out_channels: int,
+        kernel_size: Union[int, Sequence] = 3,
+        stride: Union[int, Sequence] = 1,
+        bias: bool = True,
+        transposed: bool = False,
+    ) -> None:
+        super().__init__()
+        self.in_channels = in_channels
+        self.out_channels = out_channels
+        if isinstance(kernel_size, int):
+            kernel_size = (kernel_size,) * 3
+        if isinstance(stride, int):
+            stride = (stride,) * 3
+        kernel_size = tuple(kernel_size)
+        stride = tuple(stride)
+        assert len(kernel_size) == 3 and len(stride) == 3
+        self.kernel_size = kernel_size
+        self.stride = stride
+        self.transposed = transposed
+        if self.transposed:
+            out_channels, in_channels = in_channels, out_channels
+        self.kernel_volume = math.prod(self.kernel_size)
+        if self.kernel_volume > 1:
+            weight_shape = [out_channels, in_channels] + list(self.kernel_size)
+            weight = torch.zeros(*weight_shape[::-1]).permute(4, 3, 2, 1, 0)
+            self.weight = nn.Parameter(weight)
+        else:
+            self.weight = nn.Parameter(torch.zeros(out_channels, in_channels))
+        if bias:
+            self.bias = nn.Parameter(torch.empty(self.out_channels))
+        else:
+            self.register_parameter("bias", None)
+        self.reset_parameters()
+
+    def extra_repr(self) -> str:
+        s = "{in_channels}, {out_channels}, kernel_size={kernel_size}"
+        if self.stride != (1, 1, 1):
+            s += ", stride={stride}"
+        if self.bias is None:
+            s += ", bias=False"
+        if self.transposed:
+            s += ", transposed=True"
+        return s.format(**self.__dict__)
+
+    def reset_parameters(self) -> None:
+        std = 1 / math.sqrt((self.out_channels if self.transposed else self.in_channels) * self.kernel_volume)
+        self.weight.data.uniform_(-std, std)
+        if self.bias is not None:
+            self.bias.data.uniform_(-std, std)
+
+    def _dispatch_conv(self, in_feature, in_grid: GridBatch, in_kmap, out_grid):
+        can_cache = self.stride == (1, 1, 1) and (out_grid is None or out_grid.is_same(in_grid))
+        if in_kmap is not None and in_kmap.kernel_size == self.kernel_size and can_cache:
+            kmap, out_grid = in_kmap, in_grid
+        elif self.transposed:
+            if out_grid is None:
+                raise ValueError("a transposed SparseConv3d needs out_grid")
+            kmap, _ = out_grid.sparse_conv_kernel_map(self.kernel_size, self.stride, in_grid)
+        else:
+            kmap, out_grid = in_grid.sparse_conv_kernel_map(self.kernel_size, self.stride, out_grid)
+        out_kmap = kmap if can_cache else None
+        if self.training:
+            kmap.build_implicit_gemm(sorted=False, training=False)
+        if not self.transposed:
+            out_feature = kmap.sparse_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM)
+        else:
+            out_feature = kmap.sparse_transpose_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM)
+        return out_grid, out_feature, out_kmap
+
+    def forward(self, input: VDBTensor, out_grid: Optional[GridBatch] = None) -> VDBTensor:
+        in_feature, in_grid, in_kmap = input.data, input.grid, input.kmap
+        if self.kernel_size == (1, 1, 1) and self.stride == (1, 1, 1):
+            out_feature = in_feature.jagged_like(in_feature.jdata.matmul(self.weight.transpose(0, 1)))
+            out_grid, out_kmap = in_grid, in_kmap
+        else:
+            out_grid, out_feature, out_kmap = self._dispatch_conv(in_feature, in_grid, in_kmap, out_grid)
+        if self.bias is not None:
+            out_feature.jdata = out_feature.jdata + self.bias
+        if out_grid is None:
+            raise ValueError("Failed to compute output grid. This is a bug in the implementation.")
+        return VDBTensor(out_grid, out_feature, out_kmap)
+
+
+class ReLU(nn.ReLU):
+    """Elementwise ReLU on a VDBTensor's features (grid and kernel map unchanged)."""
+
+    def forward(self, input: VDBTensor) -> VDBTensor:
+        return VDBTensor(input.grid, input.data.jagged_like(super().forward(input.data.jdata)), input.kmap)

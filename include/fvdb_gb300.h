@@ -1,0 +1,234 @@
+/*
+ * fvdb_gb300 — C ABI of the GB300 sparse-convolution path (libfvdb_gb300.so).
+ *
+ * Conventions for every entry point:
+ *   - plain C types only; every buffer is caller-allocated device memory unless the
+ *     argument says "host"; the library never allocates, frees or keeps a pointer
+ *     after returning;
+ *   - all device work is enqueued on the `stream` argument (0 = legacy default);
+ *   - return value is a status code (FVGB_OK on success); nothing throws.
+ *   - counts are int64, map entries are int32 (-1 = no neighbour), exactly as in the
+ *     reference's torch tensors.
+ *
+ * Each declaration names the reference interface it replaces (fvdb-core paths).
+ */
+#ifndef FVDB_GB300_H
+#define FVDB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void *fvgb_stream_t; /* a cudaStream_t */
+
+/* status codes; the host wrapper maps them to ValueError / TypeError / RuntimeError */
+enum {
+    FVGB_OK = 0,
+    FVGB_EINVAL = 1,   /* bad shape / size / argument          -> ValueError   */
+    FVGB_ETYPE = 2,    /* unsupported element type or layout  -> TypeError    */
+    FVGB_ERANGE = 3,   /* coordinate outside the supported box -> ValueError  */
+    FVGB_ECUDA = 4,    /* CUDA launch or runtime failure       -> RuntimeError */
+    FVGB_ETIMEOUT = 5, /* a bounded device wait gave up        -> RuntimeError */
+    FVGB_ENOSPACE = 6  /* caller workspace too small           -> RuntimeError */
+};
+
+/* element types */
+enum { FVGB_F32 = 0, FVGB_F64 = 1, FVGB_BF16 = 2, FVGB_F16 = 3, FVGB_E4M3 = 4 };
+
+/* Voxel coordinates must lie in [-2^20, 2^20) on every axis (the sort key packs nine
+ * root-tile bits per axis); grids may hold up to 2^31-1 voxels. */
+#define FVGB_COORD_LIMIT (1 << 20)
+
+/*
+ * One leaf (8x8x8 brick) of an index grid.  Voxels of a leaf are contiguous in the
+ * grid's index order; bit b = (x&7)<<6 | (y&7)<<3 | (z&7) of `mask` marks an active
+ * voxel, whose index is base + prefix[b>>6] + popcount(mask[b>>6] & ((1<<(b&63))-1)).
+ * Replaces nanovdb::OnIndexTree::LeafNodeType as used by GridBatchImpl::Accessor
+ * (src/fvdb/detail/GridBatchImpl.h:118-245).  128 bytes, 128-byte aligned.
+ */
+typedef struct FvgbLeaf {
+    int32_t origin[3]; /* coordinate of voxel (0,0,0) of the leaf, multiples of 8 */
+    int32_t batch;     /* grid of the batch this leaf belongs to */
+    int64_t base;      /* global index of the leaf's first active voxel */
+    uint16_t prefix[8];
+    uint64_t mask[8];
+    int64_t pad[4];
+} FvgbLeaf;
+
+/*
+ * A batch of index grids (a jagged GridBatch), as a view over caller-owned device
+ * memory.  Replaces fvdb::detail::GridBatchImpl's device accessor
+ * (src/fvdb/detail/GridBatchImpl.h:118-245) for the convolution path.
+ */
+typedef struct FvgbGrid {
+    int32_t num_grids;
+    int32_t reserved;
+    int64_t num_voxels;
+    int64_t num_leaves;
+    int64_t hash_capacity;        /* power of two, >= 2 * num_leaves */
+    const int64_t *voxel_offsets; /* [num_grids+1] device, int64 (fvdb joffsets) */
+    const int32_t *ijk;           /* [num_voxels,3] device, index order */
+    const FvgbLeaf *leaves;       /* [num_leaves] device, index order */
+    const int32_t *hash_slots;    /* [hash_capacity] device, leaf id or -1 */
+} FvgbGrid;
+
+/* Library version and build info (host). */
+const char *fvgb_version(void);
+/* Last CUDA error string seen by the library on this thread (host). */
+const char *fvgb_last_error(void);
+/* Number of kernels this library has launched in this process (host; library kernels of
+ * CUB used inside the grid builder are not counted). */
+uint64_t fvgb_launch_count(void);
+
+/* ---------------------------------------------------------------- grid build ----- */
+
+/*
+ * Bytes of workspace that fvgb_ijk_sort_unique needs for n input coordinates.
+ * (host, no device work)
+ */
+int fvgb_ijk_sort_unique_workspace(int64_t n, int32_t num_grids, size_t *bytes);
+
+/*
+ * Sort jagged ijk [n,3] (grid b owns rows joffsets[b]..joffsets[b+1]) into the
+ * NanoVDB OnIndex voxel order of each grid and drop duplicates.  Writes out_ijk
+ * (capacity n rows) and out_joffsets[num_grids+1] (device); the unique count is
+ * out_joffsets[num_grids].  *err_dev (device int32, zeroed by the caller) becomes
+ * FVGB_ERANGE if a coordinate is outside FVGB_COORD_LIMIT.
+ * Replaces dispatchCreateNanoGridFromIJK<kCUDA> (src/fvdb/detail/ops/BuildGridFromIjk.cu:26-83)
+ * and its nanovdb::tools::cuda::voxelsToGrid call, without the per-grid host loop.
+ */
+int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids, int64_t n,
+                         int32_t *out_ijk, int64_t *out_joffsets, int32_t *err_dev, void *workspace,
+                         size_t workspace_bytes, fvgb_stream_t stream);
+
+/*
+ * Count the leaves of sorted unique ijk: writes leaf_start[n] (device int32, 1 where a
+ * voxel starts a new leaf, exclusive-scanned in place to leaf ids) and *num_leaves_dev.
+ * workspace: fvgb_scan_workspace(n) bytes.
+ */
+int fvgb_scan_workspace(int64_t n, size_t *bytes);
+int fvgb_grid_leaf_scan(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids, int64_t n,
+                        int32_t *leaf_ids, int64_t *num_leaves_dev, void *workspace,
+                        size_t workspace_bytes, fvgb_stream_t stream);
+
+/*
+ * Fill grid->leaves and grid->hash_slots (both caller-allocated, writable through the
+ * casts) from sorted unique ijk and the leaf ids of fvgb_grid_leaf_scan.  Replaces the
+ * NanoVDB tree build + PopulateGridMetadata (src/fvdb/detail/ops/PopulateGridMetadata.cu:39-90).
+ */
+int fvgb_grid_index_build(const FvgbGrid *grid, const int32_t *leaf_ids, fvgb_stream_t stream);
+
+/*
+ * ijk of points: ijk = floor(p / voxel_size - origin / voxel_size + 0.5) per grid,
+ * points f32 [n,3], per-grid voxel_size/origin f64 [num_grids,3] (device), batch of
+ * each point from joffsets.  Replaces ijkForPoints (src/fvdb/detail/ops/BuildGridFromPoints.cu:27-43).
+ */
+int fvgb_points_to_ijk(const float *points, const int64_t *joffsets, int32_t num_grids, int64_t n,
+                       const double *voxel_sizes, const double *origins, int32_t *out_ijk,
+                       fvgb_stream_t stream);
+
+/*
+ * Candidate coordinates of conv_grid(kernel, stride) for every voxel of `grid`
+ * (k = k0*k1*k2 candidates per voxel, or one when stride==1 or stride==kernel).
+ * Writes out_ijk [num_voxels*kc, 3] and out_valid [num_voxels*kc] (uint8); the caller
+ * compacts (fvgb_compact_ijk) and sorts (fvgb_ijk_sort_unique).
+ * Replaces convIJKForGrid / dispatchCoarseIJKForFineGrid
+ * (src/fvdb/detail/ops/BuildGridForConv.cu:66-178, src/fvdb/detail/ops/CoarseIjkForFineGrid.cu:19-75).
+ */
+int fvgb_conv_grid_candidates(const FvgbGrid *grid, const int32_t ksize[3], const int32_t stride[3],
+                              int32_t *out_ijk, uint8_t *out_valid, fvgb_stream_t stream);
+
+/*
+ * Stream-compact flagged rows: out_ijk/out_joffsets get the rows of ijk whose flag is
+ * non-zero, grouped per grid (row r of the candidates belongs to grid of voxel r/per_voxel).
+ * workspace: fvgb_scan_workspace(n) bytes.
+ */
+int fvgb_compact_ijk(const int32_t *ijk, const uint8_t *valid, const int64_t *src_joffsets,
+                     int32_t num_grids, int64_t per_voxel, int64_t n, int32_t *out_ijk,
+                     int64_t *out_joffsets, void *workspace, size_t workspace_bytes,
+                     fvgb_stream_t stream);
+
+/* ---------------------------------------------------------------- kernel maps ---- */
+
+/*
+ * Kernel map: kmap[t*ld + k] = index of the source voxel at
+ * (t.x*s2 + dx, t.y*s1 + dy, t.z*s0 + dz) or -1, with the reference's offset order
+ * and axis convention (k0 and s0 act on ijk axis 2).  Rows [tgt->num_voxels, ...)
+ * are not touched.  If nbsizes (device int32[K]) is non-null, the per-offset count of
+ * valid entries is ADDED to it.
+ * Replaces dispatchConvolutionKernelMap<kCUDA>
+ * (src/fvdb/detail/ops/convolution/pack_info/ConvolutionKernelMap.cu:104-138).
+ */
+int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const int32_t ksize[3],
+                    const int32_t stride[3], int32_t *kmap, int64_t ld, int32_t *nbsizes,
+                    fvgb_stream_t stream);
+
+/*
+ * mapT[i*ldT + k] = t where kmap[t*ld + k] == i, else -1 (fills all n_in rows).
+ * Replaces dispatchTransposeOutInMap
+ * (src/fvdb/detail/ops/convolution/pack_info/IGEMMBitOperations.cu:92-105,164-182).
+ */
+int fvgb_kmap_transpose(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, int32_t *mapT,
+                        int64_t n_in, int64_t ldT, fvgb_stream_t stream);
+
+/*
+ * Gather-scatter neighbour map: nbmap[p] = (in, out) for every valid kmap entry,
+ * ordered by offset then by output row; nboffsets[k] = exclusive prefix of nbsizes
+ * (device int64[K+1], computed here).  workspace: fvgb_nbmap_workspace bytes.
+ * Replaces SparseConvPackInfo::buildGatherScatter (src/fvdb/SparseConvPackInfo.cpp:61-88).
+ */
+int fvgb_nbmap_workspace(int64_t n_out, int32_t K, size_t *bytes);
+int fvgb_nbmap_build(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, int32_t *nbmap,
+                     int64_t *nboffsets, void *workspace, size_t workspace_bytes,
+                     fvgb_stream_t stream);
+
+/*
+ * Per-row occupancy bitmask (bit k set when kmap[t,k] >= 0) for K <= 32, and the
+ * OR-reduced mask of every 128-row tile.  Replaces dispatchBitmaskFromOutInMap and
+ * dispatchReduceMask (IGEMMBitOperations.cu:14-36,54-90).
+ */
+int fvgb_kmap_masks(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, uint32_t *row_mask,
+                    uint32_t *tile_mask, fvgb_stream_t stream);
+
+/* ---------------------------------------------------------------- contractions --- */
+
+/*
+ * Forward gather-GEMM on CUDA cores, one fused pass, no atomics:
+ *   y[m, :] (+)= sum_k x[map[m*ldm + k], :] . W[k]      for m < n_out
+ * x [n_x, c_in] rows of length ldx; W element (k, ci, co) at
+ * w[k*wsk + ci*wsci + co*wsco]; y [n_out, c_out] rows of length ldy.  dtype FVGB_F32
+ * or FVGB_F64 (x, W, y all that type).  accumulate != 0 adds into y.
+ * This is the plain FP32 form (no TF32) and the FP64 form.  Together with the maps it
+ * replaces the gather -> mm -> scatter loop of dispatchSparseConvolutionKernelMap
+ * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionKernelMap.cu:116-261) and the
+ * f32 IGEMM kernels (SparseConvolutionImplicitGEMM.cu:2389-2788).
+ * Used for dgrad with the transposed map and W^T strides.
+ */
+int fvgb_conv_fwd_simt(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                       const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *w,
+                       int64_t wsk, int64_t wsci, int64_t wsco, void *y, int32_t c_out,
+                       int64_t ldy, int32_t accumulate, fvgb_stream_t stream);
+
+/*
+ * Weight gradient on CUDA cores:  dW[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co].
+ * Per-CTA FP32 (or FP64) partials go to `partials` (fvgb_wgrad_workspace bytes); the
+ * final cross-CTA reduction runs in FP64 in a fixed order (deterministic) and writes
+ * dW [K, c_in, c_out] contiguous in `dtype_out` (FVGB_F32 or FVGB_F64).
+ * Replaces the per-offset torch::mm_out(x_k^T, dy_k) of
+ * dispatchSparseConvolutionKernelMapGrad (SparseConvolutionKernelMap.cu:263-415).
+ */
+int fvgb_wgrad_workspace(int32_t dtype, int64_t n_out, int32_t K, int32_t c_in, int32_t c_out,
+                         size_t *bytes);
+int fvgb_conv_wgrad_simt(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                         const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *dy,
+                         int32_t c_out, int64_t lddy, void *dw, void *workspace,
+                         size_t workspace_bytes, fvgb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FVDB_GB300_H */

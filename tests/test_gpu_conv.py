@@ -1,0 +1,205 @@
+"""GPU parity of the contractions (FP32 plain form, FP64 form, 16-bit features) against the
+oracle, the golden fixtures and torch dense convolutions, plus the reference's error-input
+contract (tests/unit/test_conv.py:677-716)."""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as orc
+from tests.helpers import golden_cases, kernel_start, load_golden, random_sparse_ijk, rows_by_coord
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def fvdb(cuda_device):
+    import fvdb as m
+
+    return m
+
+
+def rel_max(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_config1_plain_fp32(fvdb, cuda_device):
+    """20,000 unique voxels uniform in [0,64)^3, C 16->16, 3x3x3, stride 1, FP32, no bias:
+    kernel map bit-exact; output within 1e-5 relative of the reference CPU path."""
+    g = torch.Generator().manual_seed(0)
+    idx = torch.randperm(64**3, generator=g)[:20000]
+    ijk = torch.stack([idx // 4096, (idx // 64) % 64, idx % 64], 1).to(torch.int32)
+    x = torch.randn(20000, 16, generator=g)
+    w = torch.randn(16, 16, 3, 3, 3, generator=g) * math.sqrt(1.0 / (27 * 16))
+    grid = fvdb.GridBatch.from_ijk(ijk.to(cuda_device))
+    pack, tgt = grid.sparse_conv_kernel_map(3, 1)
+    pack.build_gather_scatter()
+    o_ijk, o_off = orc.grid_from_ijk(ijk.numpy(), np.array([0, 20000]))
+    perm = [rows_by_coord(ijk.numpy())[tuple(r)] for r in o_ijk.tolist()]
+    xs = x[perm]
+    out = pack.sparse_conv_3d(xs.to(cuda_device), w.to(cuda_device), fvdb.ConvPackBackend.GATHER_SCATTER).jdata
+    kmap = orc.kernel_map(o_ijk, o_off, o_ijk, o_off, 3, 1)
+    assert np.array_equal(pack.out_in_map[:20000].cpu().numpy(), kmap)
+    nbmap, nbsizes = orc.neighbour_map(kmap)
+    ref_cpu = orc.gs_forward(xs, w, nbmap, nbsizes, 20000, middle=True).numpy()
+    got = out.cpu().numpy()
+    assert rel_max(got, ref_cpu) < 1e-5
+    assert rel_max(got, orc.conv_forward_f64(xs.numpy(), w.numpy(), kmap)) < 1e-5
+
+
+@pytest.mark.parametrize("name", golden_cases("sparse_"))
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_golden_forward(fvdb, cuda_device, name, dtype):
+    g = load_golden(name)
+    ks, st = tuple(g["kernel_size"].tolist()), tuple(g["stride"].tolist())
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(g["ijk"]).to(cuda_device))
+    pack, tgt = grid.sparse_conv_kernel_map(ks, st)
+    perm = [rows_by_coord(g["ijk"])[tuple(r)] for r in grid.ijk.jdata.cpu().numpy().tolist()]
+    x = torch.from_numpy(g["features"][perm]).to(cuda_device, dtype)
+    w = torch.from_numpy(g["weights"]).to(cuda_device, dtype)
+    out = pack.sparse_conv_3d(x, w).jdata.double().cpu().numpy()
+    order = [rows_by_coord(tgt.ijk.jdata.cpu().numpy())[tuple(r)] for r in g["target_ijk"].tolist()]
+    tol = 1e-12 if dtype == torch.float64 else 1e-5
+    assert rel_max(out[order], g["expected"]) < tol
+
+
+@pytest.mark.parametrize("name", golden_cases("dense_transposed"))
+def test_golden_transposed(fvdb, cuda_device, name):
+    g = load_golden(name)
+    ks = tuple(g["kernel_size"].tolist())
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(g["ijk"]).to(cuda_device))
+    pack, tgt = grid.sparse_conv_kernel_map(ks, 1)
+    perm = [rows_by_coord(g["ijk"])[tuple(r)] for r in grid.ijk.jdata.cpu().numpy().tolist()]
+    x = torch.from_numpy(g["features"][perm]).to(cuda_device)
+    w = torch.from_numpy(g["weights"]).to(cuda_device)
+    out = pack.sparse_transpose_conv_3d(x, w).jdata.cpu().numpy()
+    assert rel_max(out, g["expected"][perm]) < 1e-12
+
+
+CASES = [((3, 3, 3), (1, 1, 1), 16, 32), ((2, 2, 2), (2, 2, 2), 32, 16), ((3, 3, 3), (2, 2, 2), 8, 24),
+         ((5, 3, 1), (1, 3, 2), 4, 8), ((3, 3, 3), (1, 1, 1), 70, 130)]
+
+
+@pytest.mark.parametrize("ks,st,cin,cout", CASES)
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("transposed", [False, True])
+def test_forward_backward_vs_oracle(fvdb, cuda_device, ks, st, cin, cout, dtype, transposed):
+    parts = [random_sparse_ijk(2500, 20, 41, lo=-4), random_sparse_ijk(900, 14, 42, lo=30)]
+    ijk = np.concatenate(parts, 0)
+    off = np.array([0, 2500, 3400])
+    jt = fvdb.JaggedTensor.from_data_and_offsets(torch.from_numpy(ijk).to(cuda_device), torch.from_numpy(off).to(cuda_device))
+    grid = fvdb.GridBatch.from_ijk(jt)
+    pack, tgt = grid.sparse_conv_kernel_map(ks, st)
+    src, soff = orc.grid_from_ijk(ijk, off)
+    t_ijk, toff = (src, soff) if st == (1, 1, 1) else orc.conv_grid(src, soff, ks, st)
+    kmap = orc.kernel_map(src, soff, t_ijk, toff, ks, st)
+    rng = np.random.default_rng(7)
+    n_in = t_ijk.shape[0] if transposed else src.shape[0]
+    x = rng.standard_normal((n_in, cin))
+    w = rng.standard_normal(((cin, cout) if transposed else (cout, cin)) + ks) / math.sqrt(cin * np.prod(ks))
+    xt = torch.from_numpy(x).to(cuda_device, dtype).requires_grad_(True)
+    wt = torch.from_numpy(w).to(cuda_device, dtype).requires_grad_(True)
+    if transposed:
+        y = pack.sparse_transpose_conv_3d(xt, wt).jdata
+    else:
+        y = pack.sparse_conv_3d(xt, wt).jdata
+    ref = orc.conv_forward_f64(x, w, kmap, transposed=transposed, n_src=src.shape[0])
+    tol = 1e-12 if dtype == torch.float64 else 2e-5
+    assert rel_max(y.detach().double().cpu().numpy(), ref) < tol
+    dy = rng.standard_normal(ref.shape)
+    y.backward(torch.from_numpy(dy).to(cuda_device, dtype))
+    dx, dw = orc.conv_backward_f64(x, w, kmap, dy, transposed=transposed, n_src=src.shape[0])
+    assert rel_max(xt.grad.double().cpu().numpy(), dx) < tol
+    assert rel_max(wt.grad.double().cpu().numpy(), dw) < tol
+    assert wt.grad.shape == wt.shape
+
+
+@pytest.mark.parametrize("k", [2, 3, 4, 5, 6])
+@pytest.mark.parametrize("stride", [1, 2, 4])
+def test_dense_box_vs_conv3d(fvdb, cuda_device, k, stride):
+    """test_torch_sparse_conv (test_conv.py:361-461) re-hosted: from_dense box vs F.conv3d."""
+    n = 16
+    grid = fvdb.GridBatch.from_dense(1, (n, n, n), device=cuda_device)
+    torch.manual_seed(0)
+    x = torch.randn(grid.total_voxels, 4, dtype=torch.float64, device=cuda_device)
+    w = torch.randn(8, 4, k, k, k, dtype=torch.float64, device=cuda_device)
+    pack, tgt = grid.sparse_conv_kernel_map(k, stride)
+    out = pack.sparse_conv_3d(x, w).jdata
+    dense = grid.write_to_dense_xyzc(x).squeeze(0).permute(3, 2, 1, 0)
+    p = -kernel_start(k)
+    shift = 4  # targets at -1 (k=5, s=2): evaluate on a box shifted by a multiple of the stride
+    dpad = torch.nn.functional.pad(dense, (shift, k + stride, shift, k + stride, shift, k + stride))
+    ref = torch.nn.functional.conv3d(dpad[None], w, padding=p, stride=stride)[0]
+    t = tgt.ijk.jdata.long() + shift // stride
+    ref_rows = ref[:, t[:, 2], t[:, 1], t[:, 0]].T
+    assert torch.allclose(out, ref_rows, rtol=1e-12, atol=1e-12)
+
+
+def test_bf16_features_within_tolerance(fvdb, cuda_device):
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(random_sparse_ijk(20000, 48, 3)).to(cuda_device))
+    pack, _ = grid.sparse_conv_kernel_map(3, 1)
+    torch.manual_seed(1)
+    x = torch.randn(grid.total_voxels, 32, device=cuda_device)
+    w = torch.randn(64, 32, 3, 3, 3, device=cuda_device) * math.sqrt(2.0 / (27 * 32))
+    y = pack.sparse_conv_3d(x.bfloat16(), w.bfloat16()).jdata
+    assert y.dtype == torch.bfloat16
+    src = grid.ijk.jdata.cpu().numpy()
+    kmap = orc.kernel_map(src, np.array([0, src.shape[0]]), src, np.array([0, src.shape[0]]), 3, 1)
+    ref = orc.conv_forward_f64(x.bfloat16().double().cpu().numpy(), w.bfloat16().double().cpu().numpy(), kmap)
+    assert rel_l2(y.double().cpu().numpy(), ref) < 1e-2
+
+
+def test_module_forward_backward_and_kmap_cache(fvdb, cuda_device):
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(random_sparse_ijk(3000, 20, 8)).to(cuda_device))
+    conv1 = fvdb.nn.SparseConv3d(8, 16, 3).to(cuda_device)
+    conv2 = fvdb.nn.SparseConv3d(16, 8, 3).to(cuda_device)
+    x = torch.randn(grid.total_voxels, 8, device=cuda_device, requires_grad=True)
+    v = fvdb.nn.VDBTensor(grid, grid.jagged_like(x))
+    h = conv1(v)
+    assert h.kmap is not None and h.grid.is_same(grid)
+    y = conv2(fvdb.nn.ReLU()(h))
+    assert y.kmap is h.kmap  # the stride-1 map is reused, not rebuilt
+    y.data.jdata.sum().backward()
+    assert x.grad is not None and conv1.weight.grad is not None and conv1.bias.grad is not None
+    down = fvdb.nn.SparseConv3d(8, 8, 2, stride=2).to(cuda_device)(v)
+    assert down.grid.total_voxels < grid.total_voxels and down.kmap is None
+    up = fvdb.nn.SparseConv3d(8, 8, 2, stride=2, transposed=True).to(cuda_device)(down, out_grid=grid)
+    assert up.grid.is_same(grid) and up.data.jdata.shape == (grid.total_voxels, 8)
+
+
+@pytest.mark.parametrize("transposed", [False, True])
+def test_error_inputs(fvdb, cuda_device, transposed):
+    """test_error_inputs (test_conv.py:677-716): bad shapes raise ValueError."""
+    torch.manual_seed(0)
+    grid = fvdb.GridBatch.from_points(torch.randn(1000, 3, device=cuda_device), voxel_sizes=0.025, origins=[0.0, 0.0, 0.0])
+    n = grid.total_voxels
+
+    def do(feats, kernels):
+        pack, _ = grid.sparse_conv_kernel_map(kernels.shape[-1], 1)
+        pack.build_gather_scatter()
+        f = pack.sparse_transpose_conv_3d if transposed else pack.sparse_conv_3d
+        return f(feats, kernels)
+
+    with pytest.raises(ValueError):
+        do(torch.randn(n, device=cuda_device), torch.rand(8, 0, 5, 5, 5, device=cuda_device))
+    with pytest.raises(ValueError):
+        do(torch.randn(n, 5, device=cuda_device), torch.rand(8, 4, 5, 5, 5, device=cuda_device))
+    with pytest.raises(ValueError):
+        do(torch.randn(n + 7, 4, device=cuda_device), torch.rand(8, 4, 5, 5, 5, device=cuda_device))
+    with pytest.raises(TypeError):
+        do(torch.randint(0, 3, (n, 4), device=cuda_device), torch.rand(4, 4, 5, 5, 5, device=cuda_device))
+
+
+def test_empty_target_gives_empty_output(fvdb, cuda_device):
+    """test_basic_ops.py:1695-1711: an empty target grid gives an empty output with the channel count."""
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(random_sparse_ijk(100, 8, 0)).to(cuda_device))
+    empty = fvdb.GridBatch.from_ijk(torch.zeros((0, 3), dtype=torch.int32, device=cuda_device))
+    pack, _ = grid.sparse_conv_kernel_map(3, 1, empty)
+    out = pack.sparse_conv_3d(torch.randn(grid.total_voxels, 4, device=cuda_device), torch.randn(6, 4, 3, 3, 3, device=cuda_device))
+    assert out.jdata.shape == (0, 6)
