@@ -19,6 +19,8 @@ void count_launches(int n);
 inline cudaStream_t as_stream(fvgb_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
 constexpr int kLeafDim = 8;
+// find_leaf reads (origin, batch) of a leaf as one 16-byte load: leaves must stay 128 bytes.
+static_assert(sizeof(FvgbLeaf) == 128, "FvgbLeaf must be exactly 128 bytes");
 
 // ---------------------------------------------------------------------------------------
 // Voxel order key.  NanoVDB numbers the voxels of an OnIndex tree depth-first: root tiles

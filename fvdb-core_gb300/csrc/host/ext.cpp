@@ -233,6 +233,7 @@ struct PackInfo {
     std::optional<Tensor> out_in_map;      // [ceil(N_tgt/128)*128, K]
     std::optional<Tensor> out_in_map_bwd;  // [ceil(N_src/128)*128, K]
     std::optional<Tensor> nbmap, nbsizes;  // GS form
+    std::optional<Tensor> tile_mask, tile_mask_t;  // OR of row occupancy per 128-row tile (K <= 32)
     std::optional<Tensor> reorder_loc, sorted_mask, reorder_out_in_map, reduced_sorted_mask;
     std::optional<Tensor> reorder_loc_bwd, reorder_out_in_map_bwd, sorted_mask_bwd_w, sorted_mask_bwd_d;
     bool use_me = false, use_tf32 = false;
@@ -291,6 +292,27 @@ const Tensor &pack_kmap_t(PackPtr p) {
         p->out_in_map_bwd = t;
     }
     return *p->out_in_map_bwd;
+}
+
+Tensor tile_masks_of(const Tensor &map, int64_t n_rows, int32_t K) {
+    const int64_t tiles = (n_rows + 127) / 128;
+    Tensor m = torch::zeros({std::max<int64_t>(tiles, 1)}, map.options());
+    if (n_rows > 0)
+        check_status(fvgb_kmap_masks(map.data_ptr<int32_t>(), n_rows, K, K, nullptr,
+                                     reinterpret_cast<uint32_t *>(m.data_ptr<int32_t>()), cur_stream()),
+                     "kernel map tile masks");
+    return m;
+}
+
+// Per-tile occupancy of the forward map (transposed=false) or of the transposed map.
+std::optional<Tensor> pack_tile_mask(PackPtr p, bool transposed) {
+    if (p->K > 32) return std::nullopt;
+    if (!transposed) {
+        if (!p->tile_mask) p->tile_mask = tile_masks_of(pack_kmap(p), p->tgt->N, p->K);
+        return p->tile_mask;
+    }
+    if (!p->tile_mask_t) p->tile_mask_t = tile_masks_of(pack_kmap_t(p), p->src->N, p->K);
+    return p->tile_mask_t;
 }
 
 void pack_build_gather_scatter(PackPtr p, bool use_me) {
@@ -397,8 +419,31 @@ int32_t fvgb_dtype(const Tensor &t) {
     return -1;
 }
 
+// Device flag that the tensor-core kernels raise when a bounded wait gives up (per device).
+Tensor &device_error_flag(const torch::Device &dev) {
+    static std::vector<Tensor> flags(64);
+    Tensor &f = flags.at(dev.index());
+    if (!f.defined()) f = torch::zeros({1}, torch::dtype(torch::kInt32).device(dev));
+    return f;
+}
+
+// Raises if a tensor-core kernel on `dev` reported a timeout (synchronises the device).
+void check_device_errors(const torch::Device &dev) {
+    Tensor &f = device_error_flag(dev);
+    const int v = f.item<int>();
+    if (v != 0) {
+        f.zero_();
+        check_status(v, "tensor-core sparse convolution");
+    }
+}
+
+bool use_tensor_cores(const Tensor &x, int64_t cin, int64_t cout) {
+    return x.scalar_type() == torch::kBFloat16 && cin % 16 == 0 && cout <= 256 && x.stride(0) % 8 == 0;
+}
+
 // y[m] = sum_k x[map[m,k]] W[k]   for the first n_out rows of map
-Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &Wkio, bool transpose_w) {
+Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &Wkio, bool transpose_w,
+                   const std::optional<Tensor> &tile_mask = std::nullopt) {
     c10::cuda::CUDAGuard guard(x.device());
     const int64_t K = map.size(1);
     const int64_t cin = transpose_w ? Wkio.size(2) : Wkio.size(1);
@@ -409,20 +454,35 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
     Tensor w = Wkio.to(x.scalar_type());
     const int64_t wsk = w.stride(0), wsci = transpose_w ? w.stride(2) : w.stride(1), wsco = transpose_w ? w.stride(1) : w.stride(2);
     const int32_t dt = fvgb_dtype(x);
-    if (dt == FVGB_F32 || dt == FVGB_F64) {
+    auto s = cur_stream();
+    if (use_tensor_cores(x, cin, cout)) {
+        size_t wb = 0;
+        check_status(fvgb_tc_weight_bytes(FVGB_BF16, K, (int32_t)cin, (int32_t)cout, &wb), "weight pack size");
+        Tensor packed = torch::empty({(int64_t)wb}, torch::dtype(torch::kUInt8).device(x.device()));
+        check_status(fvgb_tc_pack_weights(FVGB_BF16, w.data_ptr(), K, (int32_t)cin, (int32_t)cout, wsk, wsci, wsco,
+                                          packed.data_ptr(), wb, s),
+                     "weight pack");
+        const uint32_t *tm = tile_mask ? reinterpret_cast<const uint32_t *>(tile_mask->data_ptr<int32_t>()) : nullptr;
+        check_status(fvgb_conv_fwd_tc(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
+                                      map.data_ptr<int32_t>(), n_out, (int32_t)K, tm, packed.data_ptr(), (int32_t)cout,
+                                      y.data_ptr(), y.stride(0), nullptr,
+                                      device_error_flag(x.device()).data_ptr<int32_t>(), s),
+                     "sparse conv forward (tensor cores)");
+    } else if (dt == FVGB_F32 || dt == FVGB_F64) {
         check_status(fvgb_conv_fwd_simt(dt, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0), map.data_ptr<int32_t>(),
                                         n_out, (int32_t)K, map.stride(0), w.data_ptr(), wsk, wsci, wsco, y.data_ptr(),
-                                        (int32_t)cout, y.stride(0), 0, cur_stream()),
+                                        (int32_t)cout, y.stride(0), 0, s),
                      "sparse conv forward");
     } else {
-        // 16-bit features on the CUDA-core form: FP32 accumulate, rounded once at the end.
+        // 16-bit features of shapes the tensor-core kernel does not take: CUDA cores, FP32
+        // accumulate, rounded once at the end.
         Tensor xf = x.to(torch::kFloat32), wf = w.to(torch::kFloat32);
         Tensor yf = torch::empty({n_out, cout}, xf.options());
         check_status(fvgb_conv_fwd_simt(FVGB_F32, xf.data_ptr(), xf.size(0), (int32_t)cin, xf.stride(0),
                                         map.data_ptr<int32_t>(), n_out, (int32_t)K, map.stride(0), wf.data_ptr(),
                                         wf.stride(0), transpose_w ? wf.stride(2) : wf.stride(1),
                                         transpose_w ? wf.stride(1) : wf.stride(2), yf.data_ptr(), (int32_t)cout,
-                                        yf.stride(0), 0, cur_stream()),
+                                        yf.stride(0), 0, s),
                      "sparse conv forward");
         y.copy_(yf);
     }
@@ -485,9 +545,11 @@ std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr
     }
     Tensor y;
     if (!transposed)
-        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false) : torch::empty({0, cout}, x.options());
+        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false))
+                      : torch::empty({0, cout}, x.options());
     else
-        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false) : torch::empty({0, cout}, x.options());
+        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true))
+                      : torch::empty({0, cout}, x.options());
     return {y, Wkio};
 }
 
@@ -499,10 +561,10 @@ std::vector<Tensor> conv_backward(const Tensor &dy_in, const Tensor &x, const Te
     Tensor dx, dW;
     if (!transposed) {
         // dgrad: dx[i] = sum_k dy[mapT[i,k]] W[k]^T ;  wgrad: dW[k] = sum_m x[map[m,k]]^T dy[m]
-        if (need_dx) dx = gather_gemm(dy, pack_kmap_t(p), p->src->N, Wkio, true);
+        if (need_dx) dx = gather_gemm(dy, pack_kmap_t(p), p->src->N, Wkio, true, pack_tile_mask(p, true));
         if (need_dw) dW = gather_wgrad(x, pack_kmap(p), p->tgt->N, dy, K);
     } else {
-        if (need_dx) dx = gather_gemm(dy, pack_kmap(p), p->tgt->N, Wkio, true);
+        if (need_dx) dx = gather_gemm(dy, pack_kmap(p), p->tgt->N, Wkio, true, pack_tile_mask(p, false));
         if (need_dw) dW = gather_wgrad(x, pack_kmap_t(p), p->src->N, dy, K);
     }
     if (need_dw) {
@@ -570,5 +632,6 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def_property_readonly("use_tf32", [](const PackInfo &p) { return p.use_tf32; });
 
     m.def("conv_forward", &conv_forward);
+    m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); });
     m.def("conv_backward", &conv_backward);
 }

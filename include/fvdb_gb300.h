@@ -55,7 +55,7 @@ typedef struct FvgbLeaf {
     int64_t base;      /* global index of the leaf's first active voxel */
     uint16_t prefix[8];
     uint64_t mask[8];
-    int64_t pad[4];
+    int64_t pad[3];
 } FvgbLeaf;
 
 /*
@@ -226,6 +226,43 @@ int fvgb_conv_wgrad_simt(int32_t dtype, const void *x, int64_t n_x, int32_t c_in
                          const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *dy,
                          int32_t c_out, int64_t lddy, void *dw, void *workspace,
                          size_t workspace_bytes, fvgb_stream_t stream);
+
+/* ------------------------------------------------------- tensor-core contractions --- */
+
+/*
+ * Bytes of the packed weight image that fvgb_conv_fwd_tc reads for a [K, c_in, c_out]
+ * weight in `dtype` (FVGB_BF16 or FVGB_E4M3); c_out <= 256.  (host)
+ */
+int fvgb_tc_weight_bytes(int32_t dtype, int64_t K, int32_t c_in, int32_t c_out, size_t *bytes);
+
+/*
+ * Pack W (element (k, ci, co) at w[k*wsk + ci*wsci + co*wsco], elements of `dtype`) into
+ * the tile image of fvgb_conv_fwd_tc: per (offset, 128-byte channel chunk) one
+ * [N_tile x 128 B] block in the 128B-swizzled K-major shared-memory layout, zero padded.
+ * Strides select W or W^T, so the same image format serves forward and data gradient.
+ */
+int fvgb_tc_pack_weights(int32_t dtype, const void *w, int64_t K, int32_t c_in, int32_t c_out, int64_t wsk,
+                         int64_t wsci, int64_t wsco, void *packed, size_t packed_bytes, fvgb_stream_t stream);
+
+/*
+ * Tensor-core implicit-GEMM convolution (tcgen05.mma, FP32 accumulators in TMEM):
+ *   y[m, :] = out_scale (.) sum_k x[map[m*K + k], :] . W[k]          for m < n_out
+ * x: dtype (FVGB_BF16 or FVGB_E4M3) [n_x, c_in], row stride ldx elements (16-byte rows,
+ * c_in*elem multiple of 32 bytes); map int32 [n_out, K] (-1 = absent); tile_mask: per
+ * 128-row tile the OR of the rows' occupancy bits (fvgb_kmap_masks; may be null, K <= 32
+ * only) -- offsets absent from a whole tile are skipped; packed_w from fvgb_tc_pack_weights;
+ * y: bf16 [n_out, ldy]; out_scale: per output channel FP32 factor or null.  Every output
+ * row is written once (no atomics).  *err_dev (caller-zeroed device int32) becomes
+ * FVGB_ETIMEOUT if a bounded in-kernel wait gave up.
+ * Replaces the implicit-GEMM forward kernels
+ * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionImplicitGEMM.cu:120-3826,
+ *  SparseConvolutionImplicitGEMMSorted.cu:115-4639) and, with the transposed map and the
+ * W^T image, the data gradient of SparseConvolutionImplicitGEMM::backward
+ * (src/fvdb/detail/autograd/SparseConvolutionImplicitGEMM.cpp:165-177).
+ */
+int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx, const int32_t *map,
+                     int64_t n_out, int32_t K, const uint32_t *tile_mask, const void *packed_w, int32_t c_out,
+                     void *y, int64_t ldy, const float *out_scale, int32_t *err_dev, fvgb_stream_t stream);
 
 #ifdef __cplusplus
 }

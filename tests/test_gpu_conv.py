@@ -203,3 +203,103 @@ def test_empty_target_gives_empty_output(fvdb, cuda_device):
     pack, _ = grid.sparse_conv_kernel_map(3, 1, empty)
     out = pack.sparse_conv_3d(torch.randn(grid.total_voxels, 4, device=cuda_device), torch.randn(6, 4, 3, 3, 3, device=cuda_device))
     assert out.jdata.shape == (0, 6)
+
+
+# ----------------------------------------------------------------- tensor cores (BF16) ---
+def _bf16_case(fvdb, dev, n, extent, seed, ks=(3, 3, 3), st=(1, 1, 1)):
+    ijk = random_sparse_ijk(n, extent, seed)
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(ijk).to(dev))
+    pack, tgt = grid.sparse_conv_kernel_map(ks, st)
+    src = grid.ijk.jdata.cpu().numpy()
+    t = tgt.ijk.jdata.cpu().numpy()
+    kmap = orc.kernel_map(src, np.array([0, src.shape[0]]), t, np.array([0, t.shape[0]]), ks, st)
+    return grid, pack, tgt, kmap
+
+
+@pytest.mark.parametrize(
+    "cin,cout,ks,st",
+    [(16, 16, (3, 3, 3), (1, 1, 1)), (32, 64, (3, 3, 3), (1, 1, 1)), (64, 64, (3, 3, 3), (1, 1, 1)),
+     (96, 48, (3, 3, 3), (1, 1, 1)), (128, 256, (3, 3, 3), (1, 1, 1)), (256, 128, (2, 2, 2), (2, 2, 2)),
+     (64, 200, (2, 2, 2), (2, 2, 2)), (32, 32, (5, 5, 5), (1, 1, 1)), (48, 80, (3, 1, 3), (1, 1, 1))],
+)
+def test_tensor_core_forward_bf16(fvdb, cuda_device, cin, cout, ks, st):
+    """tcgen05 forward vs the FP64 oracle on bf16-rounded inputs (tolerances written here:
+    max error <= 1e-2 of the output scale and rel-L2 <= 5e-3; bf16 output rounding is 2^-9)."""
+    grid, pack, tgt, kmap = _bf16_case(fvdb, cuda_device, 7000, 30, cin + cout, ks=ks, st=st)
+    g = torch.Generator().manual_seed(cin * 7 + cout)
+    x = torch.randn(grid.total_voxels, cin, generator=g).bfloat16()
+    w = (torch.randn((cout, cin) + ks, generator=g) * math.sqrt(2.0 / (cin * np.prod(ks)))).bfloat16()
+    y = pack.sparse_conv_3d(x.to(cuda_device), w.to(cuda_device)).jdata
+    torch.cuda.synchronize()
+    fvdb._lib.load().check_device_errors(cuda_device)
+    ref = orc.conv_forward_f64(x.double().numpy(), w.double().numpy(), kmap)
+    got = y.double().cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-2 * np.abs(ref).max()
+    assert rel_l2(got, ref) <= 5e-3
+
+
+def test_tensor_core_training_bf16(fvdb, cuda_device):
+    """BF16 forward (tcgen05), dgrad (tcgen05 over the transposed map), wgrad (FP32 partials +
+    FP64 reduction) against the FP64 oracle: rel-L2 <= 1e-2 each."""
+    grid, pack, tgt, kmap = _bf16_case(fvdb, cuda_device, 9000, 32, 5)
+    g = torch.Generator().manual_seed(5)
+    x = torch.randn(grid.total_voxels, 64, generator=g).bfloat16()
+    w = (torch.randn(64, 64, 3, 3, 3, generator=g) * math.sqrt(2.0 / (64 * 27))).bfloat16()
+    dy = torch.randn(grid.total_voxels, 64, generator=g).bfloat16()
+    xt = x.to(cuda_device).requires_grad_(True)
+    wt = w.to(cuda_device).requires_grad_(True)
+    y = pack.sparse_conv_3d(xt, wt).jdata
+    y.backward(dy.to(cuda_device))
+    ref = orc.conv_forward_f64(x.double().numpy(), w.double().numpy(), kmap)
+    dx, dw = orc.conv_backward_f64(x.double().numpy(), w.double().numpy(), kmap, dy.double().numpy())
+    assert rel_l2(y.detach().double().cpu().numpy(), ref) <= 1e-2
+    assert rel_l2(xt.grad.double().cpu().numpy(), dx) <= 1e-2
+    assert rel_l2(wt.grad.double().cpu().numpy(), dw) <= 1e-2
+
+
+def test_tensor_core_transposed_bf16(fvdb, cuda_device):
+    grid, pack, tgt, kmap = _bf16_case(fvdb, cuda_device, 6000, 28, 9, ks=(2, 2, 2), st=(2, 2, 2))
+    g = torch.Generator().manual_seed(9)
+    x = torch.randn(tgt.total_voxels, 128, generator=g).bfloat16()
+    w = (torch.randn(128, 64, 2, 2, 2, generator=g) * math.sqrt(2.0 / (128 * 8))).bfloat16()
+    y = pack.sparse_transpose_conv_3d(x.to(cuda_device), w.to(cuda_device)).jdata
+    ref = orc.conv_forward_f64(x.double().numpy(), w.double().numpy(), kmap, transposed=True, n_src=grid.total_voxels)
+    assert rel_l2(y.double().cpu().numpy(), ref) <= 5e-3
+
+
+def test_tensor_core_through_c_abi(fvdb, cuda_device):
+    """fvgb_tc_pack_weights + fvgb_conv_fwd_tc called with raw pointers."""
+    import ctypes
+
+    from fvdb import _lib
+
+    lib = _lib.cdll()
+    grid, pack, tgt, kmap = _bf16_case(fvdb, cuda_device, 4000, 24, 77)
+    n, cin, cout, K = grid.total_voxels, 32, 64, 27
+    x = torch.randn(n, cin, device=cuda_device).bfloat16()
+    wkio = (torch.randn(K, cin, cout, device=cuda_device) * 0.05).bfloat16()
+    m = torch.from_numpy(kmap).to(cuda_device)
+    nbytes = ctypes.c_size_t(0)
+    assert lib.fvgb_tc_weight_bytes(2, ctypes.c_int64(K), cin, cout, ctypes.byref(nbytes)) == 0
+    packed = torch.empty(nbytes.value, dtype=torch.uint8, device=cuda_device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.fvgb_tc_pack_weights(2, ctypes.c_void_p(wkio.data_ptr()), ctypes.c_int64(K), cin, cout,
+                                    ctypes.c_int64(cin * cout), ctypes.c_int64(cout), ctypes.c_int64(1),
+                                    ctypes.c_void_p(packed.data_ptr()), nbytes, stream) == 0
+    y = torch.empty(n, cout, device=cuda_device, dtype=torch.bfloat16)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda_device)
+    rc = lib.fvgb_conv_fwd_tc(2, ctypes.c_void_p(x.data_ptr()), ctypes.c_int64(n), cin, ctypes.c_int64(cin),
+                              ctypes.c_void_p(m.data_ptr()), ctypes.c_int64(n), K, None,
+                              ctypes.c_void_p(packed.data_ptr()), cout, ctypes.c_void_p(y.data_ptr()),
+                              ctypes.c_int64(cout), None, ctypes.c_void_p(err.data_ptr()), stream)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    w5 = wkio.double().cpu().numpy().reshape(3, 3, 3, cin, cout).transpose(4, 3, 2, 1, 0)
+    ref = orc.conv_forward_f64(x.double().cpu().numpy(), w5, kmap)
+    assert rel_l2(y.double().cpu().numpy(), ref) <= 5e-3
+    # channel counts the kernel does not take are rejected before launch
+    assert lib.fvgb_conv_fwd_tc(2, ctypes.c_void_p(x.data_ptr()), ctypes.c_int64(n), 24, ctypes.c_int64(24),
+                                ctypes.c_void_p(m.data_ptr()), ctypes.c_int64(n), K, None,
+                                ctypes.c_void_p(packed.data_ptr()), cout, ctypes.c_void_p(y.data_ptr()),
+                                ctypes.c_int64(cout), None, ctypes.c_void_p(err.data_ptr()), stream) == 1
