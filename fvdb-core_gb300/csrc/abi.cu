@@ -11,6 +11,8 @@ thread_local char g_last_error[256] = "";
 std::atomic<unsigned long long> g_launches{0};
 }
 
+void record_message(const char *msg) { snprintf(g_last_error, sizeof(g_last_error), "%s", msg); }
+
 void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 int record_cuda(cudaError_t e) {

@@ -10,6 +10,8 @@ namespace fvgb {
 
 // Records the CUDA error (if any) for fvgb_last_error and maps it to a status code.
 int record_cuda(cudaError_t e);
+// Records a library error message for fvgb_last_error (host).
+void record_message(const char *msg);
 // Status of the last launch on this thread.
 inline int launch_status() { return record_cuda(cudaGetLastError()); }
 // Adds n to the process-wide count of kernels launched by this library (CUB's

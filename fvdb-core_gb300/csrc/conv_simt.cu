@@ -263,3 +263,101 @@ extern "C" int fvgb_conv_wgrad_simt(int32_t dtype, const void *x, int64_t n_x, i
     count_launches(n_out > 0 ? 2 : 1);
     return launch_status();
 }
+
+// ---------------------------------------------------------------------------------------------
+// Weight gradient that allocates nothing.
+//
+// Some callers cannot allocate device memory at the point where they need a weight gradient:
+// plugins running inside a host runtime that plans every device buffer ahead of time and
+// forbids allocation during execution, and latency-bound serving code that must not risk the
+// implicit device synchronisation or the out-of-memory failure of cudaMalloc / cudaFree in the
+// middle of a request.  fvgb_conv_wgrad_simt needs a caller-provided partials workspace; this
+// variant keeps its per-CTA partials in a fixed device array of this file instead (4 MiB per
+// device, held by every GPU that loads the library until the process exits).
+//
+// * The device address of the array is looked up once per device, with that device current,
+//   by the first call on that device (cudaGetSymbolAddress); make that first call before any
+//   stream capture.
+// * Every call shares the one array and it keeps the previous call's contents.  Each call
+//   overwrites every partial it later reads (no clearing needed), so consecutive calls are
+//   independent -- but calls that overlap on the GPU (different streams, or concurrent host
+//   threads) race on the array and must be serialised by the caller.
+// * Sizes whose partials of one row chunk (K * c_in * c_out elements) exceed the array are
+//   rejected with FVGB_ENOSPACE before any launch.
+// ---------------------------------------------------------------------------------------------
+#include <mutex>
+
+static constexpr size_t kWgradScratchBytes = size_t(4) << 20;
+static __device__ __align__(256) double fvgb_wgrad_scratch[kWgradScratchBytes / sizeof(double)];
+
+namespace fvgb {
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of fvgb_wgrad_scratch on the current device (looked up once per device).
+int wgrad_scratch_address(void **out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return record_cuda(e);
+    if (dev < 0 || dev >= kMaxDevices) return FVGB_EINVAL;
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, fvgb_wgrad_scratch);
+        if (e != cudaSuccess) return record_cuda(e);
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return FVGB_OK;
+}
+}  // namespace
+}  // namespace fvgb
+
+extern "C" int fvgb_conv_wgrad_simt_noalloc(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                            const int32_t *map, int64_t n_out, int32_t K, int64_t ldm,
+                                            const void *dy, int32_t c_out, int64_t lddy, void *dw,
+                                            fvgb_stream_t stream) {
+    if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldm < K || ldx < c_in || lddy < c_out || !dw)
+        return FVGB_EINVAL;
+    if (dtype != FVGB_F32 && dtype != FVGB_F64) return FVGB_ETYPE;
+    const size_t elem = dtype == FVGB_F64 ? 8 : 4;
+    const size_t per_chunk_bytes = (size_t)K * (size_t)c_in * (size_t)c_out * elem;
+    const int64_t cap_chunks = (int64_t)(kWgradScratchBytes / per_chunk_bytes);
+    if (cap_chunks < 1) {
+        record_message("fvgb_conv_wgrad_simt_noalloc: K*c_in*c_out partials exceed the 4 MiB scratch array");
+        return FVGB_ENOSPACE;
+    }
+    void *scratch = nullptr;
+    const int st = wgrad_scratch_address(&scratch);
+    if (st != FVGB_OK) return st;
+    WgradPlan p = wgrad_plan(n_out, K, c_in, c_out);
+    if (p.chunks > cap_chunks) {
+        p.rows_per_chunk = ceil_div(ceil_div(n_out > 0 ? n_out : 1, cap_chunks), BK) * BK;
+        p.chunks = ceil_div(n_out > 0 ? n_out : 1, p.rows_per_chunk);
+    }
+    cudaStream_t s = as_stream(stream);
+    const int64_t per_chunk = (int64_t)K * c_in * c_out;
+    const dim3 grid((unsigned)p.chunks, (unsigned)K, (unsigned)(p.tiles_ci * p.tiles_co));
+    if (grid.y > 65535 || grid.z > 65535) return FVGB_EINVAL;
+    if (dtype == FVGB_F32) {
+        float *part = reinterpret_cast<float *>(scratch);
+        if (n_out > 0)
+            wgrad_simt_kernel<float, float><<<grid, NT, 0, s>>>((const float *)x, n_x, c_in, ldx, map, n_out, K,
+                                                               ldm, (const float *)dy, c_out, lddy,
+                                                               p.rows_per_chunk, p.tiles_co, part);
+        wgrad_reduce_kernel<float, float><<<(unsigned)ceil_div(per_chunk, 256), 256, 0, s>>>(
+            part, n_out > 0 ? p.chunks : 0, per_chunk, (float *)dw);
+    } else {
+        double *part = reinterpret_cast<double *>(scratch);
+        if (n_out > 0)
+            wgrad_simt_kernel<double, double><<<grid, NT, 0, s>>>((const double *)x, n_x, c_in, ldx, map, n_out,
+                                                                 K, ldm, (const double *)dy, c_out, lddy,
+                                                                 p.rows_per_chunk, p.tiles_co, part);
+        wgrad_reduce_kernel<double, double><<<(unsigned)ceil_div(per_chunk, 256), 256, 0, s>>>(
+            part, n_out > 0 ? p.chunks : 0, per_chunk, (double *)dw);
+    }
+    count_launches(n_out > 0 ? 2 : 1);
+    return launch_status();
+}

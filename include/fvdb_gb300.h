@@ -227,6 +227,23 @@ int fvgb_conv_wgrad_simt(int32_t dtype, const void *x, int64_t n_x, int32_t c_in
                          int32_t c_out, int64_t lddy, void *dw, void *workspace,
                          size_t workspace_bytes, fvgb_stream_t stream);
 
+/*
+ * Weight gradient that allocates nothing -- no counterpart in the reference.
+ * Same result as fvgb_conv_wgrad_simt (up to the FP32 rounding of a different chunking),
+ * for callers that cannot allocate device memory when they call it: plugins inside runtimes
+ * that plan all device memory ahead of time and forbid allocation during execution, and
+ * serving code that must not risk cudaMalloc/cudaFree synchronising the device or failing
+ * mid-request.  The partials live in a fixed 4 MiB device array of the library (every GPU
+ * that loads the library holds it until exit); sizes with K*c_in*c_out*elem > 4 MiB are
+ * rejected with FVGB_ENOSPACE before any launch.  The first call on a device looks up the
+ * array's device address for that device (make it before any stream capture).  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised by the caller.
+ * dtype FVGB_F32 or FVGB_F64; dw [K, c_in, c_out] contiguous.
+ */
+int fvgb_conv_wgrad_simt_noalloc(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                 const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *dy,
+                                 int32_t c_out, int64_t lddy, void *dw, fvgb_stream_t stream);
+
 /* ------------------------------------------------------- tensor-core contractions --- */
 
 /*
