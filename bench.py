@@ -56,11 +56,11 @@ def sphere_shell_points(n_points: int, seed: int, device) -> torch.Tensor:
     return p.to(device)
 
 
-def make_c2_inputs(device, rank: int = 0):
+def make_c2_inputs(device, rank: int = 0, n_points: int = 2_000_000):
     """ijk (jagged, int32, unsorted as voxelised) for the 4 grids."""
     ijk_parts = []
     for b in range(4):
-        p = sphere_shell_points(2_000_000, 100 + b + 1000 * rank, device)
+        p = sphere_shell_points(n_points, 100 + b + 1000 * rank, device)
         ijk = torch.floor(p * 256 + 0.5).to(torch.int32)
         ijk_parts.append(torch.unique(ijk, dim=0))
     return ijk_parts
@@ -235,7 +235,7 @@ def run_gpu(args) -> None:
     import ctypes
 
     lib.fvgb_launch_count.restype = ctypes.c_uint64
-    ijk_parts = make_c2_inputs(dev, rank)
+    ijk_parts = make_c2_inputs(dev, rank, args.points)
     off = torch.tensor([0] + [p.shape[0] for p in ijk_parts], dtype=torch.int64).cumsum(0)
     ijk = torch.cat(ijk_parts, 0)
     grid = fvdb.GridBatch.from_ijk(fvdb.JaggedTensor.from_data_and_offsets(ijk, off.to(dev)))
@@ -276,31 +276,33 @@ def run_gpu(args) -> None:
     ms = float(t_all.item())
 
     # end to end through the public API from pinned host buffers
-    ijk_host = ijk.cpu().pin_memory()
-    off_host = off.clone()
-    x_host = x.cpu().pin_memory()
-    e2e_steps = max(2, min(args.steps, 5))
-    h2d = ijk_host.numel() * 4 + x_host.numel() * 2 + off_host.numel() * 8
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record()
-    d2h = 0
-    for _ in range(e2e_steps):
-        ijk_d = ijk_host.to(dev, non_blocking=True)
-        x_d = x_host.to(dev, non_blocking=True)
-        grid_e = fvdb.GridBatch.from_ijk(fvdb.JaggedTensor.from_data_and_offsets(ijk_d, off_host.to(dev, non_blocking=True)))
-        # the voxel order of the built grid is the grid's own: features are given per input row,
-        # so they are reordered through ijk_to_index as a user would
-        idx = grid_e.ijk_to_index(fvdb.JaggedTensor.from_data_and_offsets(ijk_d, off_host.to(dev)), cumulative=True).jdata
-        x_sorted = torch.empty_like(x_d)
-        x_sorted[idx] = x_d
-        y_e, *_ = model.forward(grid_e, x_sorted)
-        out_host = y_e.to("cpu")
-        d2h = out_host.numel() * out_host.element_size()
-    t1.record()
-    torch.cuda.synchronize()
-    e2e_ms = t0.elapsed_time(t1) / e2e_steps
+    e2e_ms, h2d, d2h = float('nan'), 0, 0
+    if not args.no_e2e:
+        ijk_host = ijk.cpu().pin_memory()
+        off_host = off.clone()
+        x_host = x.cpu().pin_memory()
+        e2e_steps = max(2, min(args.steps, 5))
+        h2d = ijk_host.numel() * 4 + x_host.numel() * 2 + off_host.numel() * 8
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        d2h = 0
+        for _ in range(e2e_steps):
+            ijk_d = ijk_host.to(dev, non_blocking=True)
+            x_d = x_host.to(dev, non_blocking=True)
+            grid_e = fvdb.GridBatch.from_ijk(fvdb.JaggedTensor.from_data_and_offsets(ijk_d, off_host.to(dev, non_blocking=True)))
+            # the voxel order of the built grid is the grid's own: features are given per input row,
+            # so they are reordered through ijk_to_index as a user would
+            idx = grid_e.ijk_to_index(fvdb.JaggedTensor.from_data_and_offsets(ijk_d, off_host.to(dev)), cumulative=True).jdata
+            x_sorted = torch.empty_like(x_d)
+            x_sorted[idx] = x_d
+            y_e, *_ = model.forward(grid_e, x_sorted)
+            out_host = y_e.to("cpu")
+            d2h = out_host.numel() * out_host.element_size()
+        t1.record()
+        torch.cuda.synchronize()
+        e2e_ms = t0.elapsed_time(t1) / e2e_steps
 
     peaks = load_peaks()
     conv1_flops = 2.0 * P1 * 32 * 64
@@ -322,7 +324,7 @@ def run_gpu(args) -> None:
         "config": {"workload": WORKLOAD, "voxels": n_vox, "voxels_l2": g2.total_voxels, "pairs_l1": P1, "pairs_l2": P2,
                    "l2_policy": "inputs larger than L2 (per-step working set > 129 MB)", "parallelism": f"replicas{world}"},
         "voxels_per_s": n_vox * world / (ms * 1e-3),
-        "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12 if e2e_ms == e2e_ms else None, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "gpu_launches": int(l1 - l0),
         "clocks": clk,
@@ -357,6 +359,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--points", type=int, default=2_000_000,
+                    help="points per grid (the headline workload uses 2M; smaller only for profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1,25 +1,5 @@
-// Tensor-core (tcgen05 / TMEM) implicit-GEMM sparse convolution for sm_103a.
-//
-//   y[m, :] = scale * sum_k x[map[m,k], :] . W[k]        (BF16 or FP8-E4M3 in, FP32 accumulate)
-//
-// One CTA owns 128 output rows and all (<= 256) output channels, so every output row is
-// written exactly once, without atomics.  The reduction dimension runs over (offset k,
-// channel chunk c); offsets whose 128 map entries are all -1 (per-tile occupancy mask from
-// the kernel-map build) are skipped.
-//
-// Warp roles (160 threads):
-//   warps 0-3  gather: thread r owns row r of the tile; per step it reads map[m0+r, k] from
-//              shared memory and issues 16-byte cp.async copies of the gathered feature row
-//              straight into the 128B-swizzled K-major operand layout (zero-filled where the
-//              map is -1), then arrives on the stage's mbarrier when its copies land.  Thread 0
-//              also fetches the stage's weight tile with one bulk async copy of a pre-packed,
-//              pre-swizzled image.  After the main loop these warps are the epilogue: TMEM ->
-//              registers (tcgen05.ld) -> scale/convert -> global.
-//   warp 4     TMEM allocation and the single MMA-issuing thread (tcgen05.mma M=128, N=BN).
-//
-// Reference kernels replaced: conv_forward_cuda_setting{1,2,3}_mode{0,1}_{bf16,f16,tf32,f32}
-// (src/fvdb/detail/ops/convolution/backend/SparseConvolutionImplicitGEMM.cu:120-3826 and
-// SparseConvolutionImplicitGEMMSorted.cu:115-4639), sm_80 mma.sync code.
+// Tensor-core (tcgen05 / TMEM) weight gradient and FP8 quantisation for sm_103a.
+// (The forward / data-gradient contraction lives in conv_fwd_tc.cu.)
 #include <cuda_bf16.h>
 
 #include "tc_common.cuh"
@@ -30,57 +10,135 @@ namespace {
 using namespace tc;
 
 constexpr int kTileM = 128;
-constexpr int kRowBytes = 128;  // one swizzle row = 64 bf16 or 128 fp8 elements
 constexpr int kThreads = 160;
-constexpr int kABytes = kTileM * kRowBytes;
 
-struct TcArgs {
-    const uint8_t *x;
-    int64_t n_x;
-    int64_t ldx_bytes;
+}  // namespace
+}  // namespace fvgb
+
+using namespace fvgb;
+
+// ---------------------------------------------------------------------------------------------
+// FP8-E4M3 quantisation: out[r, c] = e4m3(x[r, c] * inv_scale[c]) (round to nearest, saturate).
+#include <cuda_fp8.h>
+
+namespace fvgb {
+namespace {
+template <typename T>
+__device__ __forceinline__ float to_f32(T v);
+template <>
+__device__ __forceinline__ float to_f32<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float to_f32<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <typename T>
+__global__ void quantize_e4m3_kernel(const T *__restrict__ x, int64_t n, int32_t c, int64_t ldx,
+                                     const float *__restrict__ inv_scale, uint8_t *__restrict__ out, int64_t ldo) {
+    const int64_t total = n * c;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / c;
+        const int32_t ch = (int32_t)(e - r * c);
+        const float v = to_f32<T>(x[r * ldx + ch]) * inv_scale[ch];
+        out[r * ldo + ch] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+    }
+}
+}  // namespace
+}  // namespace fvgb
+
+extern "C" int fvgb_quantize_e4m3(int32_t dtype, const void *x, int64_t n, int32_t c, int64_t ldx,
+                                  const float *inv_scale, void *out, int64_t ldo, fvgb_stream_t stream) {
+    if (n < 0 || c < 1 || ldx < c || ldo < c || !inv_scale || (n > 0 && (!x || !out))) return FVGB_EINVAL;
+    if (n == 0) return FVGB_OK;
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n * c, 256), 148 * 64);
+    cudaStream_t s = as_stream(stream);
+    if (dtype == FVGB_F32)
+        quantize_e4m3_kernel<float><<<blocks, 256, 0, s>>>((const float *)x, n, c, ldx, inv_scale, (uint8_t *)out, ldo);
+    else if (dtype == FVGB_BF16)
+        quantize_e4m3_kernel<__nv_bfloat16><<<blocks, 256, 0, s>>>((const __nv_bfloat16 *)x, n, c, ldx, inv_scale,
+                                                                   (uint8_t *)out, ldo);
+    else
+        return FVGB_ETYPE;
+    count_launches(1);
+    return launch_status();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Tensor-core weight gradient (BF16 in, FP32 per-CTA partials, FP64 cross-CTA reduction):
+//
+//   dW[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co]
+//
+// One CTA owns a group of G = 128 / c_in kernel offsets and a chunk of output rows.  Per stage
+// of 128 rows it gathers the G feature rows of every output row into an MN-major A operand
+// (M = G*c_in stacked offsets, K = 128 rows) and the dy rows into an MN-major B operand
+// (N = c_out), so dy is loaded once for all G offsets; D (M = 128, N = c_out) accumulates in
+// TMEM across the chunk.  Stages whose 128 rows have none of the group's offsets (per-tile
+// occupancy mask) are skipped.  The epilogue writes the chunk's partial dW slice in FP32; a
+// second kernel sums the partials over chunks in FP64 in a fixed order.
+// Replaces the split-K wgrad kernels conv_backward_cuda_setting{1,2}_mode{0,1}_*
+// (src/fvdb/detail/ops/convolution/backend/SparseConvolutionImplicitGEMMGrad.cu:115-4101,
+// ...GradSorted.cu:115-4582) and their [32, K*Cin, Cout].sum(0).
+namespace fvgb {
+namespace {
+
+constexpr int kMNAtom = 16384;  // 128 K-rows x 128 bytes: one 64-element-wide MN atom of a stage
+
+// MN-major operand, 128B swizzle: MN atoms (64 elements) kMNAtom apart (LBO), 8-row K groups
+// 1024 bytes apart (SBO).
+__device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)(kMNAtom >> 4) << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// byte offset of 16-byte piece `e8` (element index e = 8*e8 along MN) of K-row r in an MN-major stage
+__device__ __forceinline__ uint32_t mn_offset(uint32_t r, uint32_t e) {
+    return (e >> 6) * kMNAtom + (r >> 3) * 1024u + (r & 7u) * 128u + ((((e & 63u) >> 3) ^ (r & 7u)) << 4);
+}
+
+struct WgArgs {
+    const uint8_t *x;  // bf16 [n_x, cin]
+    int64_t n_x, ldx_bytes;
     int32_t cin;
     const int32_t *map;
     int64_t n_out;
     int32_t K;
-    const uint32_t *tile_mask;  // may be null (or K > 32): no skipping
-    const uint8_t *wpack;       // [K][nchunks][BN rows][128 B]
-    int32_t nchunks;
+    const uint32_t *tile_mask;
+    const uint8_t *dy;  // bf16 [n_out, cout]
+    int64_t lddy_bytes;
     int32_t cout;
-    uint8_t *y;                 // bf16 [n_out, ldy]
-    int64_t ldy;
-    const float *scale;         // per output channel, may be null
+    int64_t rows_per_chunk;  // multiple of 128
+    float *partials;         // [chunks][K][cin][cout]
     int32_t *err;
     int32_t stages;
-    int32_t stage_map;          // 1: map tile staged in shared memory (K <= 32)
 };
 
 template <int BN>
-__host__ __device__ constexpr int stage_bytes() {
-    return kABytes + BN * kRowBytes;
+__host__ __device__ constexpr int wg_stage_bytes() {
+    return 2 * kMNAtom + (BN / 64) * kMNAtom;
 }
 
-// ebytes: element size (2 = bf16, 1 = e4m3)
-template <int BN, int EBYTES>
-__global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(TcArgs a) {
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    constexpr int kStage = stage_bytes<BN>();
+    constexpr int kStage = wg_stage_bytes<BN>();
+    constexpr int kBOff = 2 * kMNAtom;
     const int S = a.stages;
-    int32_t *map_tile = reinterpret_cast<int32_t *>(smem + S * kStage);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(map_tile + (a.stage_map ? kTileM * a.K : 0));
-    uint64_t *full = bars, *empty = bars + S, *accum = bars + 2 * S;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + S * kStage);
+    uint64_t *empty = full + S, *accum = full + 2 * S;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum + 1);
     volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t m0 = (int64_t)blockIdx.x * kTileM;
-    constexpr uint32_t kTmemCols = BN < 32 ? 32 : BN;
-    constexpr int kChunkElems = kRowBytes / EBYTES;
-
-    const uint32_t kbits = a.K >= 32 ? 0xffffffffu : ((1u << a.K) - 1u);
-    const uint32_t tmask = (a.tile_mask && a.K <= 32) ? (a.tile_mask[blockIdx.x] & kbits) : kbits;
-    const int n_k = a.K <= 32 ? __popc(tmask) : a.K;
-    const int n_steps = n_k * a.nchunks;
+    const int G = 128 / a.cin;
+    const int k0 = blockIdx.x * G;
+    const int ng = min(G, a.K - k0);
+    const int64_t r_begin = (int64_t)blockIdx.y * a.rows_per_chunk;
+    const int64_t r_end = min(a.n_out, r_begin + a.rows_per_chunk);
+    const uint32_t gbits = (a.K <= 32) ? (((1u << ng) - 1u) << k0) : 0xffffffffu;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
@@ -90,133 +148,94 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(TcArgs a) {
         mbar_init(accum, 1);
         *abort = 0;
     }
-    if (warp == 4) tmem_alloc(tmem_slot, kTmemCols);
-    if (a.stage_map) {
-        for (int e = threadIdx.x; e < kTileM * a.K; e += kThreads) {
-            const int64_t row = m0 + e / a.K;
-            int32_t v = row < a.n_out ? a.map[row * a.K + (e % a.K)] : -1;
-            map_tile[e] = (v >= 0 && v < a.n_x) ? v : -1;
-        }
-    }
+    if (warp == 4) tmem_alloc(tmem_slot, BN);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    const int64_t n_tiles = (r_end - r_begin + kTileM - 1) / kTileM;
 
+    auto tile_active = [&](int64_t t) -> bool {
+        if (!a.tile_mask || a.K > 32) return true;
+        return (a.tile_mask[(r_begin / kTileM) + t] & gbits) != 0;
+    };
+
+    int steps = 0;  // active stages: the gather warps run the same loop as the MMA thread
     if (warp < 4) {
-        // ------------------------------------------------------------- gather producer
         const int r = threadIdx.x;
-        const int64_t row = m0 + r;
-        uint32_t kb = tmask;
         int it = 0;
-        for (int kk = 0; kk < n_k && !*abort; ++kk) {
-            int k;
-            if (a.K <= 32) {
-                k = __ffs(kb) - 1;
-                kb &= kb - 1;
-            } else {
-                k = kk;
-            }
-            int32_t src;
-            if (a.stage_map) {
-                src = map_tile[r * a.K + k];
-            } else {
-                src = row < a.n_out ? a.map[row * a.K + k] : -1;
-                if (src >= a.n_x) src = -1;
-            }
-            const uint8_t *src_row = src >= 0 ? a.x + (int64_t)src * a.ldx_bytes : a.x;
-            for (int c = 0; c < a.nchunks; ++c, ++it) {
-                const int stage = it % S;
-                if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) break;
-                uint8_t *As = smem + stage * kStage;
-                const int width = min(kChunkElems, a.cin - c * kChunkElems);
-                const int nch = (width * EBYTES) >> 4;
-                const uint32_t dst = smem_u32(As);
-                for (int j = 0; j < nch; ++j) {
-                    const uint8_t *g = src >= 0 ? src_row + (int64_t)c * kRowBytes + j * 16 : a.x;
-                    cp_async_16(dst + sw128_offset(r, j), g, src >= 0 ? 16u : 0u);
+        for (int64_t t = 0; t < n_tiles; ++t)
+            if (tile_active(t)) ++steps;
+        for (int64_t t = 0; t < n_tiles && !*abort; ++t) {
+            if (!tile_active(t)) continue;
+            const int stage = it % S;
+            if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) break;
+            const uint32_t base = smem_u32(smem + stage * kStage);
+            const int64_t m = r_begin + t * kTileM + r;
+            const bool row_ok = m < r_end;
+            // B: dy row m, c_out channels
+            const uint8_t *dyrow = a.dy + (row_ok ? m : 0) * a.lddy_bytes;
+            for (int e = 0; e < a.cout; e += 8)
+                cp_async_16(base + kBOff + mn_offset(r, e), dyrow + e * 2, row_ok ? 16u : 0u);
+            // A: the G gathered feature rows, stacked along M
+            for (int j = 0; j < G; ++j) {
+                int32_t src = -1;
+                if (row_ok && j < ng) {
+                    src = a.map[m * a.K + k0 + j];
+                    if (src >= a.n_x) src = -1;
                 }
-                cp_async_arrive_noinc(&full[stage]);
-                if (r == 0) {
-                    mbar_arrive_expect_tx(&full[stage], BN * kRowBytes);
-                    bulk_g2s(dst + kABytes, a.wpack + ((int64_t)k * a.nchunks + c) * (BN * kRowBytes), BN * kRowBytes,
-                             &full[stage]);
-                }
+                const uint8_t *xrow = a.x + (src >= 0 ? (int64_t)src * a.ldx_bytes : 0);
+                for (int e = 0; e < a.cin; e += 8)
+                    cp_async_16(base + mn_offset(r, j * a.cin + e), xrow + e * 2, src >= 0 ? 16u : 0u);
             }
+            cp_async_arrive_noinc(&full[stage]);
+            if (r == 0) mbar_arrive(&full[stage]);
+            ++it;
         }
         cp_async_wait_all();
     } else if (warp == 4 && lane == 0) {
-        // ------------------------------------------------------------- MMA issuer
-        constexpr uint32_t idesc = EBYTES == 2 ? idesc_m128(BN, 1, 1) : idesc_m128(BN, 0, 0);
+        constexpr uint32_t idesc = idesc_m128(BN, 1, 1) | (1u << 15) | (1u << 16);  // bf16, A and B MN-major
         int it = 0;
-        bool ok = true;
-        for (int kk = 0; kk < n_k && ok; ++kk) {
-            for (int c = 0; c < a.nchunks; ++c, ++it) {
-                const int stage = it % S;
-                if (!mbar_wait(&full[stage], (it / S) & 1, abort)) {
-                    ok = false;
-                    break;
-                }
-                fence_proxy_async();
-                tc_fence_after();
-                const uint32_t As = smem_u32(smem + stage * kStage);
-                const uint32_t Bs = As + kABytes;
-                const int width = min(kChunkElems, a.cin - c * kChunkElems);
-                const int nmma = (width * EBYTES) >> 5;  // 32 bytes of K per MMA
-                for (int q = 0; q < nmma; ++q) {
-                    const uint64_t ad = desc_sw128(As + q * 32), bd = desc_sw128(Bs + q * 32);
-                    if (EBYTES == 2)
-                        mma_f16(tmem, ad, bd, idesc, (it > 0 || q > 0) ? 1u : 0u);
-                    else
-                        mma_f8(tmem, ad, bd, idesc, (it > 0 || q > 0) ? 1u : 0u);
-                }
-                mma_commit(&empty[stage]);
-            }
+        for (int64_t t = 0; t < n_tiles; ++t) {
+            if (!tile_active(t)) continue;
+            const int stage = it % S;
+            if (!mbar_wait(&full[stage], (it / S) & 1, abort)) break;
+            fence_proxy_async();
+            tc_fence_after();
+            const uint32_t As = smem_u32(smem + stage * kStage), Bs = As + kBOff;
+#pragma unroll
+            for (int q = 0; q < kTileM / 16; ++q)  // 16 rows of K per MMA = two 8-row groups
+                mma_f16(tmem, desc_sw128_mn(As + q * 2048), desc_sw128_mn(Bs + q * 2048), idesc,
+                        (it > 0 || q > 0) ? 1u : 0u);
+            mma_commit(&empty[stage]);
+            ++it;
         }
-        if (n_steps > 0 && it > 0)
+        // it == 0: nothing accumulated -- the epilogue writes zeros
+        if (it > 0)
             mma_commit(accum);
         else
             mbar_arrive(accum);
     }
-
     if (warp < 4) {
-        // ------------------------------------------------------------- epilogue
-        // warp-uniform: tcgen05.ld below is a .sync.aligned warp instruction
         const bool have = __all_sync(0xffffffffu, mbar_wait(accum, 0, abort) && !*abort);
         tc_fence_after();
-        const int r = warp * 32 + lane;
-        const int64_t row = m0 + r;
-        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
-        __nv_bfloat16 *yrow = reinterpret_cast<__nv_bfloat16 *>(a.y) + row * a.ldy;
+        const int row = warp * 32 + lane;  // M index = j * cin + ci
+        const int j = row / a.cin, ci = row % a.cin;
+        const int k = k0 + j;
+        float *dst = a.partials + (((int64_t)blockIdx.y * a.K + k) * a.cin + ci) * a.cout;
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 16) {
             float v[16];
-            if (n_steps > 0 && have) {
-                tmem_ld16(tbase + c0, v);
+            if (have && steps > 0) {
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
             } else {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) v[i] = 0.f;
             }
-            if (row < a.n_out && have) {
-                if (c0 + 16 <= a.cout && (a.ldy % 8) == 0) {
-                    uint32_t packed[8];
+            if (have && j < ng) {
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        float lo = v[2 * i], hi = v[2 * i + 1];
-                        if (a.scale) {
-                            lo *= a.scale[c0 + 2 * i];
-                            hi *= a.scale[c0 + 2 * i + 1];
-                        }
-                        __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
-                        packed[i] = *reinterpret_cast<uint32_t *>(&h);
-                    }
-                    uint4 *dst = reinterpret_cast<uint4 *>(yrow + c0);
-                    dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-                } else {
-                    for (int i = 0; i < 16 && c0 + i < a.cout; ++i)
-                        yrow[c0 + i] = __float2bfloat16_rn(a.scale ? v[i] * a.scale[c0 + i] : v[i]);
-                }
+                for (int i = 0; i < 16; i += 4)
+                    *reinterpret_cast<float4 *>(dst + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
             }
         }
     }
@@ -224,146 +243,107 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(TcArgs a) {
     __syncthreads();
     if (warp == 4) {
         tc_fence_after();
-        tmem_dealloc(tmem, kTmemCols);
+        tmem_dealloc(tmem, BN);
     }
     if (threadIdx.x == 0 && *abort) atomicExch(a.err, FVGB_ETIMEOUT);
 }
 
-// Packed weight image: for every (k, chunk c): BN rows (output channel n) x 128 bytes holding
-// W[k][c*CE + e][n] for e in [0, CE) (CE = 128/ebytes), laid out exactly as the 128B-swizzled
-// K-major shared-memory operand (zero where c*CE+e >= cin or n >= cout).
-__global__ void pack_weights_kernel(const uint8_t *__restrict__ w, int64_t K, int32_t cin, int32_t cout,
-                                    int64_t wsk, int64_t wsci, int64_t wsco, int32_t ebytes, int32_t BN,
-                                    int32_t nchunks, uint8_t *__restrict__ out) {
-    const int64_t total = K * nchunks * BN * 128 / ebytes;  // elements of the image
-    const int ce = 128 / ebytes;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t tilei = e / ((int64_t)BN * ce);
-        const int64_t rem = e % ((int64_t)BN * ce);
-        const int n = (int)(rem / ce), kk = (int)(rem % ce);
-        const int64_t k = tilei / nchunks;
-        const int c = (int)(tilei % nchunks);
-        const int ci = c * ce + kk;
-        const uint32_t byte = (uint32_t)kk * ebytes;
-        const uint32_t off = sw128_offset((uint32_t)n, byte >> 4) + (byte & 15);
-        uint8_t *dst = out + tilei * (int64_t)BN * 128 + off;
-        const bool ok = ci < cin && n < cout;
-        const int64_t src = (k * wsk + (int64_t)ci * wsci + (int64_t)n * wsco) * ebytes;
-        if (ebytes == 2) {
-            *reinterpret_cast<uint16_t *>(dst) = ok ? *reinterpret_cast<const uint16_t *>(w + src) : (uint16_t)0;
-        } else {
-            *dst = ok ? w[src] : (uint8_t)0;
-        }
-    }
+__global__ void wgrad_reduce_f64_kernel(const float *__restrict__ partials, int64_t chunks, int64_t per_chunk,
+                                        float *__restrict__ dw) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= per_chunk) return;
+    double s = 0.0;
+    for (int64_t c = 0; c < chunks; ++c) s += (double)partials[c * per_chunk + e];
+    dw[e] = (float)s;
 }
 
-int tile_n(int32_t cout) {
-    if (cout <= 32) return 32;
-    if (cout <= 64) return 64;
-    if (cout <= 128) return 128;
-    if (cout <= 256) return 256;
-    return -1;
+struct TcWgradPlan {
+    int64_t groups, chunks, rows_per_chunk;
+};
+
+TcWgradPlan tc_wgrad_plan(int64_t n_out, int32_t K, int32_t cin) {
+    TcWgradPlan p;
+    const int G = 128 / cin;
+    p.groups = ceil_div(K, G);
+    const int64_t tiles = ceil_div(n_out > 0 ? n_out : 1, kTileM);
+    int64_t chunks = ceil_div(4 * 148, p.groups);
+    if (chunks > tiles) chunks = tiles;
+    if (chunks < 1) chunks = 1;
+    p.rows_per_chunk = ceil_div(tiles, chunks) * kTileM;
+    p.chunks = ceil_div(n_out > 0 ? n_out : 1, p.rows_per_chunk);
+    return p;
 }
 
-template <int BN, int EB>
-int launch_fwd(TcArgs a, cudaStream_t s) {
-    constexpr int kStage = stage_bytes<BN>();
-    const int map_bytes = a.stage_map ? kTileM * a.K * 4 : 0;
-    int stages = BN >= 256 ? 4 : (BN >= 128 ? 3 : 4);
-    const int extra = 1024 + map_bytes + (2 * 6 + 1) * 8 + 16;
+template <int BN>
+int launch_wgrad(WgArgs a, int64_t groups, int64_t chunks, cudaStream_t s) {
+    constexpr int kStage = wg_stage_bytes<BN>();
+    int stages = 4;
+    const int extra = 1024 + (2 * 4 + 1) * 8 + 32;
     while (stages > 2 && stages * kStage + extra > 227 * 1024) --stages;
     a.stages = stages;
     const int smem = stages * kStage + extra;
-    auto kern = conv_tc_fwd_kernel<BN, EB>;
+    auto kern = conv_tc_wgrad_kernel<BN>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
         return launch_status();
-    const int64_t tiles = ceil_div(a.n_out, kTileM);
-    kern<<<(unsigned)tiles, kThreads, smem, s>>>(a);
-    count_launches(1);
+    kern<<<dim3((unsigned)groups, (unsigned)chunks), kThreads, smem, s>>>(a);
     return launch_status();
 }
 
 }  // namespace
 }  // namespace fvgb
 
-using namespace fvgb;
-
-extern "C" int fvgb_tc_weight_bytes(int32_t dtype, int64_t K, int32_t cin, int32_t cout, size_t *bytes) {
-    if (!bytes || K < 1 || cin < 1 || cout < 1) return FVGB_EINVAL;
-    const int eb = dtype == FVGB_E4M3 ? 1 : (dtype == FVGB_BF16 ? 2 : 0);
-    if (!eb) return FVGB_ETYPE;
-    const int BN = tile_n(cout);
-    if (BN < 0) return FVGB_EINVAL;
-    const int64_t nchunks = ceil_div((int64_t)cin * eb, 128);
-    *bytes = (size_t)(K * nchunks * BN * 128);
+extern "C" int fvgb_tc_wgrad_workspace(int64_t n_out, int32_t K, int32_t c_in, int32_t c_out, size_t *bytes) {
+    if (!bytes || K < 1 || n_out < 0 || (c_in != 32 && c_in != 64 && c_in != 128) ||
+        (c_out != 64 && c_out != 128 && c_out != 256))
+        return FVGB_EINVAL;
+    const TcWgradPlan p = tc_wgrad_plan(n_out, K, c_in);
+    *bytes = (size_t)p.chunks * K * c_in * c_out * 4 + 256;
     return FVGB_OK;
 }
 
-extern "C" int fvgb_tc_pack_weights(int32_t dtype, const void *w, int64_t K, int32_t cin, int32_t cout, int64_t wsk,
-                                    int64_t wsci, int64_t wsco, void *packed, size_t packed_bytes,
-                                    fvgb_stream_t stream) {
+extern "C" int fvgb_conv_wgrad_tc(const void *x, int64_t n_x, int32_t c_in, int64_t ldx, const int32_t *map,
+                                  int64_t n_out, int32_t K, const uint32_t *tile_mask, const void *dy, int32_t c_out,
+                                  int64_t lddy, float *dw, void *workspace, size_t workspace_bytes, int32_t *err_dev,
+                                  fvgb_stream_t stream) {
     size_t need = 0;
-    int st = fvgb_tc_weight_bytes(dtype, K, cin, cout, &need);
+    int st = fvgb_tc_wgrad_workspace(n_out, K, c_in, c_out, &need);
     if (st) return st;
-    if (!w || !packed || packed_bytes < need) return FVGB_EINVAL;
-    const int eb = dtype == FVGB_E4M3 ? 1 : 2;
-    const int BN = tile_n(cout);
-    const int nchunks = (int)ceil_div((int64_t)cin * eb, 128);
-    const int64_t total = (int64_t)need / eb;
-    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(total, 256), 4096);
-    pack_weights_kernel<<<blocks, 256, 0, as_stream(stream)>>>((const uint8_t *)w, K, cin, cout, wsk, wsci, wsco, eb, BN,
-                                                               nchunks, (uint8_t *)packed);
-    count_launches(1);
-    return launch_status();
-}
-
-extern "C" int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
-                                const int32_t *map, int64_t n_out, int32_t K, const uint32_t *tile_mask,
-                                const void *packed_w, int32_t c_out, void *y, int64_t ldy, const float *out_scale,
-                                int32_t *err_dev, fvgb_stream_t stream) {
-    const int eb = dtype == FVGB_E4M3 ? 1 : (dtype == FVGB_BF16 ? 2 : 0);
-    if (!eb) return FVGB_ETYPE;
-    if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldx < c_in || ldy < c_out || !err_dev)
-        return FVGB_EINVAL;
-    // each MMA consumes 32 bytes of K and every gathered row is copied in 16-byte pieces
-    if (((int64_t)c_in * eb) % 32 != 0 || (ldx * eb) % 16 != 0) return FVGB_EINVAL;
-    const int BN = tile_n(c_out);
-    if (BN < 0) return FVGB_EINVAL;
-    if (n_out == 0) return FVGB_OK;
-    if (!map || !packed_w || !y || (n_x > 0 && !x)) return FVGB_EINVAL;
-    if (((uintptr_t)x & 15) || ((uintptr_t)packed_w & 15) || ((uintptr_t)y & 15)) return FVGB_EINVAL;
-    TcArgs a;
-    // with no input rows every map entry is -1 and nothing is read; keep a valid address anyway
-    a.x = (const uint8_t *)(n_x > 0 ? x : y);
-    a.n_x = n_x;
-    a.ldx_bytes = ldx * eb;
-    a.cin = c_in;
-    a.map = map;
-    a.n_out = n_out;
-    a.K = K;
-    a.tile_mask = tile_mask;
-    a.wpack = (const uint8_t *)packed_w;
-    a.nchunks = (int32_t)ceil_div((int64_t)c_in * eb, 128);
-    a.cout = c_out;
-    a.y = (uint8_t *)y;
-    a.ldy = ldy;
-    a.scale = out_scale;
-    a.err = err_dev;
-    a.stages = 0;
-    a.stage_map = K <= 32 ? 1 : 0;
+    if (!dw || !err_dev || ldx < c_in || lddy < c_out || (ldx % 8) || (lddy % 8) || n_x < 0) return FVGB_EINVAL;
+    if (!workspace || workspace_bytes < need) return FVGB_ENOSPACE;
+    if (((uintptr_t)x & 15) || ((uintptr_t)dy & 15)) return FVGB_EINVAL;
+    const TcWgradPlan p = tc_wgrad_plan(n_out, K, c_in);
     cudaStream_t s = as_stream(stream);
-    if (eb == 2) {
-        switch (BN) {
-            case 32: return launch_fwd<32, 2>(a, s);
-            case 64: return launch_fwd<64, 2>(a, s);
-            case 128: return launch_fwd<128, 2>(a, s);
-            default: return launch_fwd<256, 2>(a, s);
+    float *part = reinterpret_cast<float *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    const int64_t per_chunk = (int64_t)K * c_in * c_out;
+    int launched = 0;
+    if (n_out > 0) {
+        WgArgs a;
+        a.x = (const uint8_t *)(n_x > 0 ? x : dy);
+        a.n_x = n_x;
+        a.ldx_bytes = ldx * 2;
+        a.cin = c_in;
+        a.map = map;
+        a.n_out = n_out;
+        a.K = K;
+        a.tile_mask = tile_mask;
+        a.dy = (const uint8_t *)dy;
+        a.lddy_bytes = lddy * 2;
+        a.cout = c_out;
+        a.rows_per_chunk = p.rows_per_chunk;
+        a.partials = part;
+        a.err = err_dev;
+        a.stages = 0;
+        if (p.chunks > 65535) return FVGB_EINVAL;
+        switch (c_out) {
+            case 64: st = launch_wgrad<64>(a, p.groups, p.chunks, s); break;
+            case 128: st = launch_wgrad<128>(a, p.groups, p.chunks, s); break;
+            default: st = launch_wgrad<256>(a, p.groups, p.chunks, s); break;
         }
+        if (st) return st;
+        launched = 1;
     }
-    switch (BN) {
-        case 32: return launch_fwd<32, 1>(a, s);
-        case 64: return launch_fwd<64, 1>(a, s);
-        case 128: return launch_fwd<128, 1>(a, s);
-        default: return launch_fwd<256, 1>(a, s);
-    }
+    wgrad_reduce_f64_kernel<<<(unsigned)ceil_div(per_chunk, 256), 256, 0, s>>>(part, n_out > 0 ? p.chunks : 0,
+                                                                               per_chunk, dw);
+    count_launches(launched + 1);
+    return launch_status();
 }

@@ -106,6 +106,10 @@ __global__ void leaf_flags_kernel(const int32_t *__restrict__ ijk, const int64_t
                                   int32_t B, int64_t n, int32_t *__restrict__ flags) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (i >= joff[B]) {  // n is a capacity; the voxel count lives on the device
+        flags[i] = 0;
+        return;
+    }
     int32_t f = 1;
     if (i > 0) {
         const int32_t b0 = batch_of(joff, B, i - 1), b1 = batch_of(joff, B, i);
@@ -116,8 +120,12 @@ __global__ void leaf_flags_kernel(const int32_t *__restrict__ ijk, const int64_t
     flags[i] = f;
 }
 
-__global__ void leaf_count_kernel(const int32_t *__restrict__ ids, int64_t n, int64_t *__restrict__ out) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *out = n > 0 ? (int64_t)ids[n - 1] : 0;  // inclusive scan
+__global__ void leaf_count_kernel(const int32_t *__restrict__ ids, const int64_t *__restrict__ joff, int32_t B,
+                                  int64_t *__restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int64_t n = joff[B];
+    out[0] = n > 0 ? (int64_t)ids[n - 1] : 0;  // inclusive scan
+    out[1] = n;
 }
 
 __global__ void leaf_fill_kernel(const int32_t *__restrict__ ijk, const int64_t *__restrict__ joff,
@@ -183,10 +191,12 @@ __global__ void conv_candidates_kernel(FvgbGrid g, int3 ks, int3 st, int coarse,
     if (i >= g.num_voxels) return;
     const int32_t x = g.ijk[3 * i], y = g.ijk[3 * i + 1], z = g.ijk[3 * i + 2];
     if (coarse) {
-        // floor(ijk / stride) with the stride Coord applied x<->s0 (CoarseIjkForFineGrid.cu:34-35)
-        out[3 * i] = (int32_t)floor((double)x / st.x);
-        out[3 * i + 1] = (int32_t)floor((double)y / st.y);
-        out[3 * i + 2] = (int32_t)floor((double)z / st.z);
+        // floor(ijk / stride) with the stride Coord applied x<->s0 (CoarseIjkForFineGrid.cu:34-35),
+        // in integer arithmetic (exact for int32 inputs; avoids FP64 on the device)
+        auto fdiv = [](int32_t a, int32_t b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
+        out[3 * i] = fdiv(x, st.x);
+        out[3 * i + 1] = fdiv(y, st.y);
+        out[3 * i + 2] = fdiv(z, st.z);
         valid[i] = 1;
         return;
     }
@@ -315,7 +325,7 @@ extern "C" int fvgb_grid_leaf_scan(const int32_t *ijk, const int64_t *joffsets, 
         leaf_flags_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, joffsets, num_grids, n, flags);
         cub::DeviceScan::InclusiveSum(tmp, tb, flags, leaf_ids, n, s);
     }
-    leaf_count_kernel<<<1, 32, 0, s>>>(leaf_ids, n, num_leaves_dev);
+    leaf_count_kernel<<<1, 32, 0, s>>>(leaf_ids, joffsets, num_grids, num_leaves_dev);
     count_launches(n > 0 ? 2 : 1);
     return launch_status();
 }
@@ -389,5 +399,31 @@ extern "C" int fvgb_compact_ijk(const int32_t *ijk, const uint8_t *valid, const 
     compact_offsets_kernel<<<(unsigned)ceil_div(num_grids + 1, kThreads), kThreads, 0, s>>>(
         src_joffsets, num_grids, per_voxel, flags, out_joffsets);
     count_launches(3);
+    return launch_status();
+}
+
+namespace fvgb {
+namespace {
+__global__ void ijk_to_index_kernel(FvgbGrid g, const int32_t *__restrict__ q, const int64_t *__restrict__ qoff,
+                                    int64_t n, int32_t cumulative, int64_t *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t b = batch_of(qoff, g.num_grids, i);
+    const int32_t x = q[3 * i], y = q[3 * i + 1], z = q[3 * i + 2];
+    int64_t idx = -1;
+    const int32_t id = find_leaf(g, b, x >> 3, y >> 3, z >> 3);
+    if (id >= 0) idx = leaf_voxel_index(g.leaves[id], leaf_bit(x, y, z));
+    if (idx >= 0 && !cumulative) idx -= g.voxel_offsets[b];
+    out[i] = idx;
+}
+}  // namespace
+}  // namespace fvgb
+
+extern "C" int fvgb_ijk_to_index(const FvgbGrid *grid, const int32_t *ijk, const int64_t *joffsets, int64_t n,
+                                 int32_t cumulative, int64_t *out, fvgb_stream_t stream) {
+    if (!grid || n < 0 || !joffsets || (n > 0 && (!ijk || !out))) return FVGB_EINVAL;
+    if (n == 0) return FVGB_OK;
+    ijk_to_index_kernel<<<blocks_for(n), kThreads, 0, as_stream(stream)>>>(*grid, ijk, joffsets, n, cumulative, out);
+    count_launches(1);
     return launch_status();
 }

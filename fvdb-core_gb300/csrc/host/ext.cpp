@@ -126,23 +126,25 @@ GridPtr build_grid(const Tensor &ijk_in, const Tensor &joff_in, const Tensor &vs
                                       n, out_ijk.data_ptr<int32_t>(), out_joff.data_ptr<int64_t>(),
                                       err.data_ptr<int32_t>(), ws.data_ptr(), ws.numel(), s),
                  "grid build (sort)");
-    Tensor host = torch::cat({out_joff, err.to(torch::kInt64)}).cpu();
-    TORCH_CHECK_VALUE(host[B + 1].item<int64_t>() == 0, "voxel coordinates must lie in [-2^20, 2^20)");
+    // leaf ids over the capacity n (the unique count stays on the device), so the unique count,
+    // the leaf count and the range check come back to the host in one copy
+    Tensor leaf_ids = torch::empty({std::max<int64_t>(n, 1)}, i32);
+    Tensor counts = torch::zeros({2}, torch::dtype(torch::kInt64).device(dev));
+    size_t sb = 0;
+    check_status(fvgb_scan_workspace(n, &sb), "grid build (scan workspace)");
+    Tensor ws2 = workspace(sb, dev);
+    check_status(fvgb_grid_leaf_scan(n ? out_ijk.data_ptr<int32_t>() : nullptr, out_joff.data_ptr<int64_t>(), (int32_t)B,
+                                     n, leaf_ids.data_ptr<int32_t>(), counts.data_ptr<int64_t>(), ws2.data_ptr(),
+                                     ws2.numel(), s),
+                 "grid build (leaf scan)");
+    Tensor host = torch::cat({out_joff, counts, err.to(torch::kInt64)}).cpu();
+    const int64_t *h = host.data_ptr<int64_t>();
+    TORCH_CHECK_VALUE(h[B + 3] == 0, "voxel coordinates must lie in [-2^20, 2^20)");
     g->joffsets_host = host.narrow(0, 0, B + 1).contiguous();
     g->joffsets = out_joff;
-    g->N = g->joffsets_host[B].item<int64_t>();
+    g->N = h[B];
     g->ijk = out_ijk.narrow(0, 0, g->N);
-    // leaves
-    Tensor leaf_ids = torch::empty({std::max<int64_t>(g->N, 1)}, i32);
-    Tensor nleaf = torch::zeros({1}, torch::dtype(torch::kInt64).device(dev));
-    size_t sb = 0;
-    check_status(fvgb_scan_workspace(g->N, &sb), "grid build (scan workspace)");
-    Tensor ws2 = workspace(sb, dev);
-    check_status(fvgb_grid_leaf_scan(g->N ? g->ijk.data_ptr<int32_t>() : nullptr, g->joffsets.data_ptr<int64_t>(),
-                                     (int32_t)B, g->N, leaf_ids.data_ptr<int32_t>(), nleaf.data_ptr<int64_t>(),
-                                     ws2.data_ptr(), ws2.numel(), s),
-                 "grid build (leaf scan)");
-    g->L = nleaf.item<int64_t>();
+    g->L = h[B + 1];
     g->cap = next_pow2(2 * g->L);
     g->leaves = torch::empty({std::max<int64_t>(g->L, 1) * (int64_t)sizeof(FvgbLeaf)}, torch::dtype(torch::kUInt8).device(dev));
     g->hash = torch::empty({g->cap}, i32);
@@ -216,6 +218,20 @@ GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, cons
     return build_grid(ijk, joff, g->voxel_sizes, g->origins);
 }
 
+Tensor grid_ijk_to_index(const GridPtr &g, const Tensor &ijk_in, const Tensor &joff_in, bool cumulative) {
+    c10::cuda::CUDAGuard guard(g->device());
+    TORCH_CHECK_VALUE(ijk_in.dim() == 2 && ijk_in.size(1) == 3, "ijk must have shape (N, 3)");
+    Tensor q = ijk_in.to(g->device(), torch::kInt32).contiguous();
+    Tensor qo = joff_in.to(g->device(), torch::kInt64).contiguous();
+    TORCH_CHECK_VALUE(qo.size(0) == g->B + 1, "ijk must have one list per grid");
+    Tensor out = torch::empty({q.size(0)}, torch::dtype(torch::kInt64).device(g->device()));
+    FvgbGrid v = g->view();
+    check_status(fvgb_ijk_to_index(&v, q.data_ptr<int32_t>(), qo.data_ptr<int64_t>(), q.size(0), cumulative ? 1 : 0,
+                                   out.data_ptr<int64_t>(), cur_stream()),
+                 "ijk_to_index");
+    return out;
+}
+
 Tensor grid_jidx(const GridPtr &g) {
     if (!g->jidx_cache.defined()) {
         Tensor counts = (g->joffsets_host.narrow(0, 1, g->B) - g->joffsets_host.narrow(0, 0, g->B));
@@ -264,20 +280,32 @@ PackPtr make_pack(const std::vector<int64_t> &ks_in, const std::vector<int64_t> 
     return p;
 }
 
-Tensor build_kmap(const GridPtr &src, const GridPtr &tgt, const Vec3 &ks, const Vec3 &st, int32_t K) {
+// Kernel map [ceil(N_tgt/128)*128, K] (padding rows -1); for K <= 32 the per-128-row-tile
+// occupancy masks come out of the same pass into *tile_mask.
+Tensor build_kmap(const GridPtr &src, const GridPtr &tgt, const Vec3 &ks, const Vec3 &st, int32_t K,
+                  Tensor *tile_mask = nullptr) {
     c10::cuda::CUDAGuard guard(tgt->device());
     TORCH_CHECK_VALUE(src->B == tgt->B, "source and target grids must have the same grid count");
     const int64_t npad = (tgt->N + 127) / 128 * 128;
     Tensor kmap = torch::empty({npad, K}, torch::dtype(torch::kInt32).device(tgt->device()));
     if (npad > tgt->N) kmap.narrow(0, tgt->N, npad - tgt->N).fill_(-1);
+    uint32_t *tm = nullptr;
+    if (tile_mask && K <= 32) {
+        *tile_mask = torch::zeros({std::max<int64_t>(npad / 128, 1)}, kmap.options());
+        tm = reinterpret_cast<uint32_t *>(tile_mask->data_ptr<int32_t>());
+    }
     FvgbGrid s = src->view(), t = tgt->view();
-    check_status(fvgb_kmap_build(&s, &t, ks.v, st.v, kmap.data_ptr<int32_t>(), K, nullptr, cur_stream()),
+    check_status(fvgb_kmap_build(&s, &t, ks.v, st.v, kmap.data_ptr<int32_t>(), K, nullptr, tm, cur_stream()),
                  "kernel map build");
     return kmap;
 }
 
 const Tensor &pack_kmap(PackPtr p) {
-    if (!p->out_in_map) p->out_in_map = build_kmap(p->src, p->tgt, p->ks, p->st, p->K);
+    if (!p->out_in_map) {
+        Tensor tm;
+        p->out_in_map = build_kmap(p->src, p->tgt, p->ks, p->st, p->K, &tm);
+        if (tm.defined()) p->tile_mask = tm;
+    }
     return *p->out_in_map;
 }
 
@@ -437,8 +465,12 @@ void check_device_errors(const torch::Device &dev) {
     }
 }
 
+// Shapes the tcgen05 contraction takes: 32-byte multiples of K per MMA, and rows shorter than
+// one 128-byte swizzle row must tile it (c_in 16 or 32 for bf16; any multiple of 16 from 64).
 bool use_tensor_cores(const Tensor &x, int64_t cin, int64_t cout) {
-    return x.scalar_type() == torch::kBFloat16 && cin % 16 == 0 && cout <= 256 && x.stride(0) % 8 == 0;
+    const int64_t row = cin * 2;
+    return x.scalar_type() == torch::kBFloat16 && row % 32 == 0 && (row >= 128 || 128 % row == 0) && cout <= 256 &&
+           x.stride(0) % 8 == 0;
 }
 
 // y[m] = sum_k x[map[m,k]] W[k]   for the first n_out rows of map
@@ -490,9 +522,26 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
 }
 
 // dW[k] = sum_m x[map[m,k]]^T dy[m]   -> [K, Cin, Cout]
-Tensor gather_wgrad(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &dy, int64_t K) {
+Tensor gather_wgrad(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &dy, int64_t K,
+                    const std::optional<Tensor> &tile_mask = std::nullopt) {
     c10::cuda::CUDAGuard guard(x.device());
     const int64_t cin = x.size(1), cout = dy.size(1);
+    if (x.scalar_type() == torch::kBFloat16 && (cin == 32 || cin == 64 || cin == 128) &&
+        (cout == 64 || cout == 128 || cout == 256)) {
+        // tensor cores: FP32 partials per CTA, FP64 reduction across CTAs
+        Tensor xx = x.contiguous(), dd = dy.to(torch::kBFloat16).contiguous();
+        Tensor dw = torch::empty({K, cin, cout}, x.options().dtype(torch::kFloat32));
+        size_t wsb = 0;
+        check_status(fvgb_tc_wgrad_workspace(n_out, (int32_t)K, (int32_t)cin, (int32_t)cout, &wsb), "wgrad workspace");
+        Tensor ws = workspace(wsb, x.device());
+        const uint32_t *tm = tile_mask ? reinterpret_cast<const uint32_t *>(tile_mask->data_ptr<int32_t>()) : nullptr;
+        check_status(fvgb_conv_wgrad_tc(xx.data_ptr(), xx.size(0), (int32_t)cin, xx.stride(0), map.data_ptr<int32_t>(),
+                                        n_out, (int32_t)K, tm, dd.data_ptr(), (int32_t)cout, dd.stride(0),
+                                        dw.data_ptr<float>(), ws.data_ptr(), ws.numel(),
+                                        device_error_flag(x.device()).data_ptr<int32_t>(), cur_stream()),
+                     "sparse conv weight gradient (tensor cores)");
+        return dw.to(x.scalar_type());
+    }
     const bool wide = x.scalar_type() == torch::kFloat64;
     Tensor xx = wide ? x : x.to(torch::kFloat32).contiguous();
     Tensor dd = (wide ? dy : dy.to(torch::kFloat32)).contiguous();
@@ -562,16 +611,67 @@ std::vector<Tensor> conv_backward(const Tensor &dy_in, const Tensor &x, const Te
     if (!transposed) {
         // dgrad: dx[i] = sum_k dy[mapT[i,k]] W[k]^T ;  wgrad: dW[k] = sum_m x[map[m,k]]^T dy[m]
         if (need_dx) dx = gather_gemm(dy, pack_kmap_t(p), p->src->N, Wkio, true, pack_tile_mask(p, true));
-        if (need_dw) dW = gather_wgrad(x, pack_kmap(p), p->tgt->N, dy, K);
+        if (need_dw) dW = gather_wgrad(x, pack_kmap(p), p->tgt->N, dy, K, pack_tile_mask(p, false));
     } else {
         if (need_dx) dx = gather_gemm(dy, pack_kmap(p), p->tgt->N, Wkio, true, pack_tile_mask(p, false));
-        if (need_dw) dW = gather_wgrad(x, pack_kmap_t(p), p->src->N, dy, K);
+        if (need_dw) dW = gather_wgrad(x, pack_kmap_t(p), p->src->N, dy, K, pack_tile_mask(p, true));
     }
     if (need_dw) {
         dW = dW.reshape({p->ks.v[2], p->ks.v[1], p->ks.v[0], cin, cout});
         dW = transposed ? dW.permute({3, 4, 2, 1, 0}) : dW.permute({4, 3, 2, 1, 0});
     }
     return {dx, dW};
+}
+
+// FP8-E4M3 forward (inference): per-input-channel feature scales s_x (folded into the weights)
+// and per-output-channel weight scales s_w (applied in the epilogue), FP32 accumulation:
+//   y[m, co] = s_w[co] * sum_k sum_ci e4m3(x[., ci] / s_x[ci]) * e4m3(s_x[ci] W[k, ci, co] / s_w[co])
+// Returns (y bf16, s_x, s_w).
+std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed) {
+    TORCH_CHECK_VALUE(x.dim() == 2 && x.is_cuda() && x.is_floating_point(), "features must be a 2-D CUDA float tensor");
+    TORCH_CHECK_VALUE(weights.dim() == 5, "Expected kernels to have 5 dimensions");
+    c10::cuda::CUDAGuard guard(x.device());
+    const int64_t cin = transposed ? weights.size(0) : weights.size(1);
+    const int64_t cout = transposed ? weights.size(1) : weights.size(0);
+    TORCH_CHECK_VALUE(x.size(1) == cin, "Expected input channels of kernels (", cin, ") to equal input channels of features: ",
+                      x.size(1));
+    TORCH_CHECK_VALUE(cin % 32 == 0 && cout <= 256, "the FP8 path needs in_channels % 32 == 0 and out_channels <= 256");
+    const int64_t n_rows = transposed ? p->src->N : p->tgt->N;
+    TORCH_CHECK_VALUE(x.size(0) == (transposed ? p->tgt->N : p->src->N),
+                      "The number of input features must match the number of voxels");
+    Tensor Wkio = (transposed ? weights.permute({4, 3, 2, 0, 1}) : weights.permute({4, 3, 2, 1, 0}))
+                      .reshape({-1, cin, cout})
+                      .to(torch::kFloat32);
+    const int64_t K = Wkio.size(0);
+    Tensor xc = x.scalar_type() == torch::kBFloat16 ? x.contiguous() : x.to(torch::kFloat32).contiguous();
+    Tensor s_x = (xc.size(0) > 0 ? xc.abs().amax(0).to(torch::kFloat32) : torch::ones({cin}, Wkio.options()))
+                     .clamp_min(1e-12) / 448.0f;
+    Tensor wf = Wkio * s_x.view({1, cin, 1});
+    Tensor s_w = wf.abs().amax({0, 1}).clamp_min(1e-12) / 448.0f;
+    Tensor w8 = (wf / s_w.view({1, 1, cout})).to(at::ScalarType::Float8_e4m3fn).contiguous();
+    Tensor x8 = torch::empty({xc.size(0), cin}, x.options().dtype(torch::kUInt8));
+    Tensor inv = (1.0f / s_x).contiguous();
+    auto s = cur_stream();
+    check_status(fvgb_quantize_e4m3(xc.scalar_type() == torch::kBFloat16 ? FVGB_BF16 : FVGB_F32, xc.data_ptr(),
+                                    xc.size(0), (int32_t)cin, xc.stride(0), inv.data_ptr<float>(), x8.data_ptr(), cin, s),
+                 "fp8 quantisation");
+    Tensor y = torch::empty({n_rows, cout}, x.options().dtype(torch::kBFloat16));
+    if (n_rows == 0) return {y, s_x, s_w};
+    size_t wb = 0;
+    check_status(fvgb_tc_weight_bytes(FVGB_E4M3, K, (int32_t)cin, (int32_t)cout, &wb), "weight pack size");
+    Tensor packed = torch::empty({(int64_t)wb}, x.options().dtype(torch::kUInt8));
+    check_status(fvgb_tc_pack_weights(FVGB_E4M3, w8.data_ptr(), K, (int32_t)cin, (int32_t)cout, cin * cout, cout, 1,
+                                      packed.data_ptr(), wb, s),
+                 "fp8 weight pack");
+    const Tensor &map = transposed ? pack_kmap_t(p) : pack_kmap(p);
+    auto tm = pack_tile_mask(p, transposed);
+    Tensor sw = s_w.contiguous();
+    check_status(fvgb_conv_fwd_tc(FVGB_E4M3, x8.data_ptr(), x8.size(0), (int32_t)cin, cin, map.data_ptr<int32_t>(), n_rows,
+                                  (int32_t)K, tm ? reinterpret_cast<const uint32_t *>(tm->data_ptr<int32_t>()) : nullptr,
+                                  packed.data_ptr(), (int32_t)cout, y.data_ptr(), y.stride(0), sw.data_ptr<float>(),
+                                  device_error_flag(x.device()).data_ptr<int32_t>(), s),
+                 "sparse conv forward (fp8 tensor cores)");
+    return {y, s_x, s_w};
 }
 
 std::optional<Tensor> opt(const std::optional<Tensor> &t) { return t; }
@@ -601,7 +701,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def_property_readonly("leaves", [](const GridImpl &g) { return g.leaves; })
         .def_property_readonly("hash", [](const GridImpl &g) { return g.hash; })
         .def_property_readonly("device", [](const GridImpl &g) { return g.device(); })
-        .def("jidx", [](GridPtr g) { return grid_jidx(g); });
+        .def("jidx", [](GridPtr g) { return grid_jidx(g); })
+        .def("ijk_to_index", &grid_ijk_to_index);
 
     py::class_<PackInfo, PackPtr>(m, "PackInfoImpl")
         .def(py::init([](std::vector<int64_t> k, std::vector<int64_t> s, GridPtr src, std::optional<GridPtr> tgt) {
@@ -632,6 +733,7 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def_property_readonly("use_tf32", [](const PackInfo &p) { return p.use_tf32; });
 
     m.def("conv_forward", &conv_forward);
+    m.def("conv_forward_fp8", &conv_forward_fp8);
     m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); });
     m.def("conv_backward", &conv_backward);
 }

@@ -17,8 +17,8 @@
 namespace fvgb {
 namespace {
 
-constexpr int kKmapThreads = 256;
-constexpr int kMaxWindow = 216;  // 6x6x6 source leaves (e.g. k<=9, stride<=4)
+constexpr int kKmapThreads = 128;
+constexpr int kMaxWindow = 216;  // 6x6x6 source leaves (e.g. k<=9, stride<=4); larger: hash per entry
 constexpr int kMaxKSmem = 1024;  // per-offset counters kept in shared memory
 
 struct KmapParams {
@@ -30,6 +30,8 @@ struct KmapParams {
     int64_t ld;
     int32_t *kmap;
     int32_t *nbsizes;
+    uint32_t *tile_mask;    // OR of row occupancy per 128-row tile (K <= 32), may be null
+    int32_t window;         // source leaves staged per CTA (0: not staged)
 };
 
 struct WinLeaf {
@@ -42,10 +44,14 @@ __device__ inline uint32_t win_prefix(const WinLeaf &w, uint32_t word) {
     return (w.prefix[word >> 1] >> ((word & 1) * 16)) & 0xffffu;
 }
 
+// Shared memory: WinLeaf[window] | uint16 slots[512] | int32 counts[K] | uint32 tmask[8]
 __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
-    __shared__ WinLeaf win[kMaxWindow];
-    __shared__ uint16_t slots[512];
-    __shared__ int32_t counts[kMaxKSmem];
+    extern __shared__ __align__(16) uint8_t kmap_smem[];
+    WinLeaf *win = reinterpret_cast<WinLeaf *>(kmap_smem);
+    uint16_t *slots = reinterpret_cast<uint16_t *>(win + p.window);
+    int32_t *counts = reinterpret_cast<int32_t *>(slots + 512);
+    const int nk_smem = p.nbsizes ? min(p.K, kMaxKSmem) : 0;
+    uint32_t *tmask = reinterpret_cast<uint32_t *>(counts + nk_smem);
     __shared__ int32_t s_count;
 
     const int64_t leaf_id = blockIdx.x;
@@ -60,10 +66,11 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
     const int32_t lx0 = lo_x >> 3, ly0 = lo_y >> 3, lz0 = lo_z >> 3;
     const int32_t wx = (hi_x >> 3) - lx0 + 1, wy = (hi_y >> 3) - ly0 + 1, wz = (hi_z >> 3) - lz0 + 1;
     const int32_t W = wx * wy * wz;
-    const bool staged = W <= kMaxWindow;
+    const bool staged = W <= p.window;
 
     if (threadIdx.x == 0) s_count = 0;
-    for (int k = threadIdx.x; k < p.K && k < kMaxKSmem; k += blockDim.x) counts[k] = 0;
+    if (threadIdx.x < 8) tmask[threadIdx.x] = 0;
+    for (int k = threadIdx.x; k < nk_smem; k += blockDim.x) counts[k] = 0;
     if (staged) {
         for (int w = threadIdx.x; w < W; w += blockDim.x) {
             const int32_t ix = w / (wy * wz), iy = (w / wz) % wy, iz = w % wz;
@@ -96,6 +103,7 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
     const int32_t cnt = s_count;
     const int64_t total = (int64_t)cnt * p.K;
     const int32_t K01 = p.K0 * p.K1;
+    const int64_t t0 = tbase >> 7;  // first 128-row tile this leaf's rows touch
     for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
         const int32_t r = (int32_t)(e / p.K), k = (int32_t)(e - (int64_t)r * p.K);
         const uint32_t s = slots[r];
@@ -121,15 +129,19 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
             if (id >= 0) idx = leaf_voxel_index(p.src.leaves[id], leaf_bit(sx, sy, sz));
         }
         p.kmap[(tbase + r) * p.ld + k] = (int32_t)idx;
-        if (p.nbsizes && idx >= 0) {
-            if (k < kMaxKSmem) atomicAdd(&counts[k], 1);
-            else atomicAdd(p.nbsizes + k, 1);
+        if (idx >= 0) {
+            if (p.nbsizes) {
+                if (k < kMaxKSmem) atomicAdd(&counts[k], 1);
+                else atomicAdd(p.nbsizes + k, 1);
+            }
+            if (p.tile_mask) atomicOr(&tmask[((tbase + r) >> 7) - t0], 1u << k);
         }
     }
-    if (p.nbsizes) {
+    if (p.nbsizes || p.tile_mask) {
         __syncthreads();
-        for (int k = threadIdx.x; k < p.K && k < kMaxKSmem; k += blockDim.x)
+        for (int k = threadIdx.x; k < nk_smem; k += blockDim.x)
             if (counts[k]) atomicAdd(p.nbsizes + k, counts[k]);
+        if (p.tile_mask && threadIdx.x < 8 && tmask[threadIdx.x]) atomicOr(p.tile_mask + t0 + threadIdx.x, tmask[threadIdx.x]);
     }
 }
 
@@ -220,15 +232,17 @@ using namespace fvgb;
 
 extern "C" int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const int32_t ksize[3],
                                const int32_t stride[3], int32_t *kmap, int64_t ld, int32_t *nbsizes,
-                               fvgb_stream_t stream) {
+                               uint32_t *tile_mask, fvgb_stream_t stream) {
     if (!src || !tgt || !ksize || !stride) return FVGB_EINVAL;
     for (int a = 0; a < 3; ++a)
         if (ksize[a] < 1 || stride[a] < 1) return FVGB_EINVAL;
     if (src->num_grids != tgt->num_grids) return FVGB_EINVAL;
     const int64_t K = (int64_t)ksize[0] * ksize[1] * ksize[2];
     if (K > (1 << 20) || ld < K) return FVGB_EINVAL;
+    if (tile_mask && K > 32) return FVGB_EINVAL;
     if (tgt->num_voxels == 0 || tgt->num_leaves == 0) return FVGB_OK;
     if (!kmap) return FVGB_EINVAL;
+    if (tgt->num_leaves > INT32_MAX) return FVGB_EINVAL;
     KmapParams p;
     p.src = *src;
     p.tgt = *tgt;
@@ -242,8 +256,15 @@ extern "C" int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const i
     p.ld = ld;
     p.kmap = kmap;
     p.nbsizes = nbsizes;
-    if (tgt->num_leaves > INT32_MAX) return FVGB_EINVAL;
-    kmap_leaf_kernel<<<(unsigned)tgt->num_leaves, kKmapThreads, 0, as_stream(stream)>>>(p);
+    p.tile_mask = tile_mask;
+    // The source-leaf window of a target leaf has the same extent for every leaf (leaf origins
+    // are multiples of 8, so origin*stride is too): size shared memory to it.
+    auto span = [](int32_t s, int32_t st, int32_t k) { return ((7 * s + st + k - 1) >> 3) - (st >> 3) + 1; };
+    const int64_t W = (int64_t)span(p.S2, p.st2, p.K2) * span(p.S1, p.st1, p.K1) * span(p.S0, p.st0, p.K0);
+    p.window = W <= kMaxWindow ? (int32_t)W : 0;
+    const int nk_smem = nbsizes ? (int)std::min<int64_t>(K, kMaxKSmem) : 0;
+    const size_t smem = (size_t)p.window * sizeof(WinLeaf) + 512 * sizeof(uint16_t) + nk_smem * 4 + 8 * 4;
+    kmap_leaf_kernel<<<(unsigned)tgt->num_leaves, kKmapThreads, smem, as_stream(stream)>>>(p);
     count_launches(1);
     return launch_status();
 }

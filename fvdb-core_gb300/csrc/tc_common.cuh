@@ -59,6 +59,32 @@ __device__ __forceinline__ void cp_async_16(uint32_t dst, const void *src, uint3
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_size) : "memory");
 }
 
+// L2 eviction-priority policies for cache-hinted loads.
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// cp_async_16 with an L2 cache-policy hint.
+__device__ __forceinline__ void cp_async_16_hint(uint32_t dst, const void *src, uint32_t src_size, uint64_t pol) {
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2, %3;" ::"r"(dst), "l"(src), "r"(src_size),
+                 "l"(pol)
+                 : "memory");
+}
+
+// Read-only 32-bit load that does not allocate in L1, with an L2 cache-policy hint.
+__device__ __forceinline__ int32_t ld_nc_hint(const int32_t *p, uint64_t pol) {
+    int32_t v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
 // Arrive on `bar` once all prior cp.async of this thread have completed (counted in the init count).
 __device__ __forceinline__ void cp_async_arrive_noinc(uint64_t *bar) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");

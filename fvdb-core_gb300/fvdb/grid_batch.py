@@ -272,29 +272,12 @@ class GridBatch:
         return self.read_from_dense_xyzc(dense_data.permute(0, 4, 3, 2, 1), dense_origins)
 
     def ijk_to_index(self, ijk, cumulative: bool = False) -> JaggedTensor:
-        """Index of each queried coordinate in its grid (-1 where absent)."""
+        """Index of each queried coordinate in its grid (-1 where absent); one leaf-hash probe each."""
         if isinstance(ijk, torch.Tensor):
             ijk = JaggedTensor(ijk)
         if ijk.num_outer_lists() != self.grid_count:
             raise ValueError("ijk must have one list per grid")
-        own = self._impl.ijk.to(torch.int64)
-        q = ijk.jdata.to(self.device, torch.int64)
-        qb = ijk.jidx.to(self.device, torch.int64)
-
-        def key(c, b):
-            c = c + (1 << 20)
-            return ((b * (1 << 21) + c[:, 0]) * (1 << 21) + c[:, 1]) * (1 << 21) + c[:, 2]
-
-        k_own = key(own, self.jidx.to(torch.int64))
-        srt, perm = torch.sort(k_own)
-        kq = key(q, qb)
-        pos = torch.searchsorted(srt, kq).clamp(max=max(srt.numel() - 1, 0))
-        hit = srt.numel() > 0
-        found = (srt[pos] == kq) if hit else torch.zeros_like(kq, dtype=torch.bool)
-        idx = torch.where(found, perm[pos] if hit else kq, torch.full_like(kq, -1))
-        if not cumulative:
-            base = self._impl.joffsets[:-1].to(torch.int64)[qb]
-            idx = torch.where(idx >= 0, idx - base, idx)
+        idx = self._impl.ijk_to_index(ijk.jdata, ijk.joffsets, bool(cumulative))
         return ijk.jagged_like(idx)
 
     def to(self, device) -> "GridBatch":

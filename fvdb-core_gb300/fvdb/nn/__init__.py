@@ -1,6 +1,6 @@
 """Neural-network layers of the sparse-convolution path."""
 
-from .modules import ReLU, SparseConv3d
+from .modules import RecomputeSequential, ReLU, Sequential, SparseConv3d
 from .vdbtensor import VDBTensor
 
-__all__ = ["SparseConv3d", "ReLU", "VDBTensor"]
+__all__ = ["SparseConv3d", "ReLU", "Sequential", "RecomputeSequential", "VDBTensor"]

@@ -92,10 +92,11 @@ class SparseConv3d(nn.Module):
         out_kmap = kmap if can_cache else None
         if self.training:
             kmap.build_implicit_gemm(sorted=False, training=False)
+        prec = None if self.precision == "native" else self.precision
         if not self.transposed:
-            out_feature = kmap.sparse_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM)
+            out_feature = kmap.sparse_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM, precision=prec)
         else:
-            out_feature = kmap.sparse_transpose_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM)
+            out_feature = kmap.sparse_transpose_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM, precision=prec)
         return out_grid, out_feature, out_kmap
 
     def forward(self, input: VDBTensor, out_grid: Optional[GridBatch] = None) -> VDBTensor:
@@ -117,3 +118,31 @@ class ReLU(nn.ReLU):
 
     def forward(self, input: VDBTensor) -> VDBTensor:
         return VDBTensor(input.grid, input.data.jagged_like(super().forward(input.data.jdata)), input.kmap)
+
+
+class Sequential(nn.Sequential):
+    """nn.Sequential over VDBTensor-to-VDBTensor layers."""
+
+
+class RecomputeSequential(nn.Sequential):
+    """Sequential stack whose intermediate activations are not kept for backward: the forward
+    runs under torch.utils.checkpoint (non-reentrant) and is re-run during backward.  Kernel
+    maps are cached in the VDBTensors, so the re-run repeats only the contractions; only the
+    stack's input features stay alive between forward and backward."""
+
+    def forward(self, input: VDBTensor) -> VDBTensor:
+        from torch.utils.checkpoint import checkpoint
+
+        box: dict = {}
+
+        def run(x: torch.Tensor) -> torch.Tensor:
+            kmap = box.get("in_kmap", input.kmap)
+            out = nn.Sequential.forward(self, VDBTensor(input.grid, input.grid.jagged_like(x), kmap))
+            box.setdefault("out", out)
+            if "in_kmap" not in box and out.kmap is not None and out.grid.is_same(input.grid):
+                box["in_kmap"] = out.kmap  # reused by the re-run in backward
+            return out.data.jdata
+
+        y = checkpoint(run, input.data.jdata, use_reentrant=False)
+        out = box["out"]
+        return VDBTensor(out.grid, out.grid.jagged_like(y), out.kmap)

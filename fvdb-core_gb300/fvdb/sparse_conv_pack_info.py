@@ -50,6 +50,19 @@ def _vec(v) -> list[int]:
     return v * 3 if len(v) == 1 else v
 
 
+def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, precision: str | None) -> torch.Tensor:
+    if precision in (None, "native"):
+        return sparse_conv(data, weights, impl, transposed)
+    if precision == "bf16":
+        return sparse_conv(data.to(torch.bfloat16), weights.to(torch.bfloat16), impl, transposed)
+    if precision == "fp8":
+        if torch.is_grad_enabled() and (data.requires_grad or weights.requires_grad):
+            raise RuntimeError("the FP8 convolution is forward-only; use precision='bf16' for training")
+        y, _, _ = _lib.load().conv_forward_fp8(data, weights, impl, transposed)
+        return y
+    raise ValueError(f"precision must be one of None, 'native', 'bf16', 'fp8' (got {precision!r})")
+
+
 class SparseConvPackInfo:
     def __init__(self, kernel_size=None, stride=None, source_grid=None, target_grid=None, impl=None):
         if impl is not None:
@@ -111,20 +124,36 @@ class SparseConvPackInfo:
             raise ValueError("Input element count must match target grid total voxels")
         return data
 
-    def sparse_conv_3d(self, input, weights: torch.Tensor, backend: ConvPackBackend = ConvPackBackend.GATHER_SCATTER):
-        """out[t] = sum_k in[kmap[t,k]] . W[:, :, k]  on the target grid (weights (Do, Di, K0, K1, K2))."""
+    def sparse_conv_3d(
+        self,
+        input,
+        weights: torch.Tensor,
+        backend: ConvPackBackend = ConvPackBackend.GATHER_SCATTER,
+        *,
+        precision: str | None = None,
+    ):
+        """out[t] = sum_k in[kmap[t,k]] . W[:, :, k]  on the target grid (weights (Do, Di, K0, K1, K2)).
+
+        ``precision`` (extension, default: the features' dtype): "bf16" casts features and
+        weights to BF16 (tcgen05, FP32 accumulate); "fp8" quantises them to E4M3 with
+        per-channel scales (forward only, BF16 output)."""
         src = self._impl.source_grid
         data = self._features(input, src.grid_count, src.total_voxels)
-        out = sparse_conv(data, weights, self._impl, False)
+        out = _apply(data, weights, self._impl, False, precision)
         return JaggedTensor.from_data_and_offsets(out, self._impl.target_grid.joffsets)
 
     def sparse_transpose_conv_3d(
-        self, input, weights: torch.Tensor, backend: ConvPackBackend = ConvPackBackend.GATHER_SCATTER
+        self,
+        input,
+        weights: torch.Tensor,
+        backend: ConvPackBackend = ConvPackBackend.GATHER_SCATTER,
+        *,
+        precision: str | None = None,
     ):
         """Transposed convolution from the target grid back onto the source grid (weights (Di, Do, K0, K1, K2))."""
         tgt = self._impl.target_grid
         data = self._features(input, tgt.grid_count, tgt.total_voxels)
-        out = sparse_conv(data, weights, self._impl, True)
+        out = _apply(data, weights, self._impl, True, precision)
         return JaggedTensor.from_data_and_offsets(out, self._impl.source_grid.joffsets)
 
     # ---------------------------------------------------------------- devices -----------

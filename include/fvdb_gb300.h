@@ -105,8 +105,10 @@ int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t nu
                          size_t workspace_bytes, fvgb_stream_t stream);
 
 /*
- * Count the leaves of sorted unique ijk: writes leaf_start[n] (device int32, 1 where a
- * voxel starts a new leaf, exclusive-scanned in place to leaf ids) and *num_leaves_dev.
+ * Leaf ids of sorted unique ijk: leaf_ids[i] = 1 + id of the leaf of voxel i (inclusive scan
+ * of leaf starts).  n is a capacity (>= joffsets[num_grids], the voxel count, read on the
+ * device), so this can run straight after fvgb_ijk_sort_unique without a host round trip.
+ * num_leaves_dev (device int64[2]) receives {leaf count, voxel count}.
  * workspace: fvgb_scan_workspace(n) bytes.
  */
 int fvgb_scan_workspace(int64_t n, size_t *bytes);
@@ -120,6 +122,15 @@ int fvgb_grid_leaf_scan(const int32_t *ijk, const int64_t *joffsets, int32_t num
  * NanoVDB tree build + PopulateGridMetadata (src/fvdb/detail/ops/PopulateGridMetadata.cu:39-90).
  */
 int fvgb_grid_index_build(const FvgbGrid *grid, const int32_t *leaf_ids, fvgb_stream_t stream);
+
+/*
+ * Index of each query coordinate (query q belongs to grid b with joffsets[b] <= q <
+ * joffsets[b+1]) in `grid`, or -1 where the grid has no voxel; global (cumulative != 0) or
+ * per-grid index.  One leaf-hash probe per query.  Replaces GridBatch::ijk_to_index
+ * (src/fvdb/GridBatch.cpp, dispatchIjkToIndex) for the convolution path's callers.
+ */
+int fvgb_ijk_to_index(const FvgbGrid *grid, const int32_t *ijk, const int64_t *joffsets, int64_t n,
+                      int32_t cumulative, int64_t *out, fvgb_stream_t stream);
 
 /*
  * ijk of points: ijk = floor(p / voxel_size - origin / voxel_size + 0.5) per grid,
@@ -158,13 +169,15 @@ int fvgb_compact_ijk(const int32_t *ijk, const uint8_t *valid, const int64_t *sr
  * (t.x*s2 + dx, t.y*s1 + dy, t.z*s0 + dz) or -1, with the reference's offset order
  * and axis convention (k0 and s0 act on ijk axis 2).  Rows [tgt->num_voxels, ...)
  * are not touched.  If nbsizes (device int32[K]) is non-null, the per-offset count of
- * valid entries is ADDED to it.
+ * valid entries is ADDED to it.  If tile_mask (device uint32[ceil(N_tgt/128)], zeroed by the
+ * caller; K <= 32) is non-null, bit k of tile_mask[t] is set when any row of the 128-row tile
+ * t has a neighbour at offset k (the occupancy mask the contractions use to skip offsets).
  * Replaces dispatchConvolutionKernelMap<kCUDA>
  * (src/fvdb/detail/ops/convolution/pack_info/ConvolutionKernelMap.cu:104-138).
  */
 int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const int32_t ksize[3],
                     const int32_t stride[3], int32_t *kmap, int64_t ld, int32_t *nbsizes,
-                    fvgb_stream_t stream);
+                    uint32_t *tile_mask, fvgb_stream_t stream);
 
 /*
  * mapT[i*ldT + k] = t where kmap[t*ld + k] == i, else -1 (fills all n_in rows).
@@ -280,6 +293,30 @@ int fvgb_tc_pack_weights(int32_t dtype, const void *w, int64_t K, int32_t c_in, 
 int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx, const int32_t *map,
                      int64_t n_out, int32_t K, const uint32_t *tile_mask, const void *packed_w, int32_t c_out,
                      void *y, int64_t ldy, const float *out_scale, int32_t *err_dev, fvgb_stream_t stream);
+
+/*
+ * Tensor-core weight gradient, BF16 operands:  dw[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co]
+ * (FP32, [K, c_in, c_out] contiguous).  c_in in {32, 64, 128} (128/c_in offsets share one
+ * M=128 MMA), c_out in {64, 128, 256}; rows of x and dy 16-byte aligned.  Per-CTA FP32
+ * partials go to `workspace` (fvgb_tc_wgrad_workspace bytes) and are summed across CTAs in
+ * FP64 in a fixed order (deterministic).  tile_mask as for fvgb_conv_fwd_tc (may be null).
+ * Replaces the split-K implicit-GEMM wgrad
+ * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionImplicitGEMMGrad.cu:115-4101,
+ *  SparseConvolutionImplicitGEMMGradSorted.cu:115-4582).
+ */
+int fvgb_tc_wgrad_workspace(int64_t n_out, int32_t K, int32_t c_in, int32_t c_out, size_t *bytes);
+int fvgb_conv_wgrad_tc(const void *x, int64_t n_x, int32_t c_in, int64_t ldx, const int32_t *map, int64_t n_out,
+                       int32_t K, const uint32_t *tile_mask, const void *dy, int32_t c_out, int64_t lddy, float *dw,
+                       void *workspace, size_t workspace_bytes, int32_t *err_dev, fvgb_stream_t stream);
+
+/*
+ * FP8-E4M3 quantisation of features: out[r, c] = e4m3_satfinite(x[r, c] * inv_scale[c]),
+ * x FVGB_F32 or FVGB_BF16 [n, c] (row stride ldx), out uint8 [n, ldo].  Per-channel scales
+ * of the FP8 convolution (the reference has no FP8 path; its closest interface is the
+ * dtype dispatch of SparseConvolutionImplicitGEMM.cu:2788-3826).
+ */
+int fvgb_quantize_e4m3(int32_t dtype, const void *x, int64_t n, int32_t c, int64_t ldx, const float *inv_scale,
+                       void *out, int64_t ldo, fvgb_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -278,7 +278,10 @@ def test_tensor_core_through_c_abi(fvdb, cuda_device):
     n, cin, cout, K = grid.total_voxels, 32, 64, 27
     x = torch.randn(n, cin, device=cuda_device).bfloat16()
     wkio = (torch.randn(K, cin, cout, device=cuda_device) * 0.05).bfloat16()
-    m = torch.from_numpy(kmap).to(cuda_device)
+    npad = (n + 127) // 128 * 128  # the reference's out_in_map layout: rows padded to 128 with -1
+    m = torch.full((npad, K), -1, dtype=torch.int32)
+    m[:n] = torch.from_numpy(kmap)
+    m = m.to(cuda_device)
     nbytes = ctypes.c_size_t(0)
     assert lib.fvgb_tc_weight_bytes(2, ctypes.c_int64(K), cin, cout, ctypes.byref(nbytes)) == 0
     packed = torch.empty(nbytes.value, dtype=torch.uint8, device=cuda_device)

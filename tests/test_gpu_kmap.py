@@ -144,17 +144,26 @@ def test_kmap_through_c_abi(fvdb, cuda_device):
     ks = (ctypes.c_int32 * 3)(3, 3, 3)
     st = (ctypes.c_int32 * 3)(1, 1, 1)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    n_tiles = (impl.total_voxels + 127) // 128
+    tmask = torch.zeros(n_tiles, dtype=torch.int32, device=cuda_device)
     rc = lib.fvgb_kmap_build(ctypes.byref(g), ctypes.byref(g), ks, st, ctypes.c_void_p(kmap.data_ptr()),
-                             ctypes.c_int64(K), ctypes.c_void_p(sizes.data_ptr()), stream)
+                             ctypes.c_int64(K), ctypes.c_void_p(sizes.data_ptr()), ctypes.c_void_p(tmask.data_ptr()),
+                             stream)
     assert rc == 0
     torch.cuda.synchronize()
     src, soff = orc.grid_from_ijk(ijk, off)
     o = orc.kernel_map(src, soff, src, soff, (3, 3, 3), (1, 1, 1))
     assert np.array_equal(kmap.cpu().numpy(), o)
     assert np.array_equal(sizes.cpu().numpy(), (o >= 0).sum(0))
+    # per-128-row-tile occupancy masks, computed in the same pass
+    bits = ((o >= 0).astype(np.int64) << np.arange(K)).sum(1)
+    pad = np.zeros(n_tiles * 128, dtype=np.int64)
+    pad[: bits.size] = bits
+    expect = np.bitwise_or.reduce(pad.reshape(n_tiles, 128), axis=1)
+    assert np.array_equal(tmask.cpu().numpy().astype(np.int64) & 0xFFFFFFFF, expect)
     # bad arguments are rejected before any launch
     assert lib.fvgb_kmap_build(ctypes.byref(g), ctypes.byref(g), ks, st, ctypes.c_void_p(kmap.data_ptr()),
-                               ctypes.c_int64(5), None, stream) == 1
+                               ctypes.c_int64(5), None, None, stream) == 1
 
 
 def test_from_points_and_empty(fvdb, cuda_device):
