@@ -215,6 +215,16 @@ def run_reference(args) -> None:
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------------ replicas ------------
+def max_over_ranks(value: float, dist=None, device="cpu") -> float:
+    """Max of a per-rank timing over all ranks (replicas: the job takes as long as the slowest)."""
+    if dist is None:
+        return float(value)
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------------ GPU arm -------------
 def run_gpu(args) -> None:
     import fvdb
@@ -270,10 +280,7 @@ def run_gpu(args) -> None:
     clk = clocks.stop()
     ms = start.elapsed_time(end) / args.steps
     conv_ms = statistics.median(a.elapsed_time(b) for a, b in ev)
-    t_all = torch.tensor([ms], device=dev)
-    if dist:
-        dist.all_reduce(t_all, op=dist.ReduceOp.MAX)
-    ms = float(t_all.item())
+    ms = max_over_ranks(ms, dist, dev)
 
     # end to end through the public API from pinned host buffers
     e2e_ms, h2d, d2h = float('nan'), 0, 0
@@ -346,10 +353,202 @@ def run_gpu(args) -> None:
         line["cpu_baseline"] = {"value": r["flops"] / r["seconds"] / 1e12, "unit": "TFLOP/s", "cores": torch.get_num_threads(),
                                 "kind": "port",
                                 "sample": f"layer 1 (3^3 32->64) of grid 0 restricted to {r['voxels']} voxels, fp32, kernel map + gather/torch.mm/scatter ({r['seconds']:.2f} s)"}
+    if not args.no_extras:
+        line["fp32_plain"] = leg_fp32(fvdb, grid, x, model, flops, args)
+        line["bf16_vs_fp32"] = tf / line["fp32_plain"]["value"] if line["fp32_plain"]["value"] else None
+        line["train_c3"] = leg_train(fvdb, dev, args)
+        line["fp8_c4"] = leg_fp8(fvdb, dev, args)
+        line["serving_c5"] = leg_serve(fvdb, dev, args)
     if rank == 0:
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ extra legs ----------
+def time_ms(fn, steps: int, warmup: int) -> float:
+    for _ in range(max(warmup, 1)):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def rel_errors(got: torch.Tensor, ref: torch.Tensor) -> dict:
+    d = (got.double() - ref.double())
+    return {"rel_l2": float(d.norm() / ref.double().norm().clamp_min(1e-300)),
+            "max_abs": float(d.abs().max()), "max_rel_to_scale": float(d.abs().max() / ref.double().abs().max().clamp_min(1e-300))}
+
+
+def leg_fp32(fvdb, grid, x, model, flops, args) -> dict:
+    """The same two-layer step in the plain FP32 form (CUDA-core FFMA, no TF32): the x1 of BF16."""
+    w1, w2 = model.w1.float(), model.w2.float()
+    xf = x.float()
+
+    def step():
+        p1, _ = grid.sparse_conv_kernel_map(3, 1)
+        h = p1.sparse_conv_3d(xf, w1).jdata
+        p2, _ = grid.sparse_conv_kernel_map(2, 2)
+        p2.sparse_conv_3d(h, w2)
+
+    ms = time_ms(step, max(2, args.steps // 2), 1)
+    return {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms, "dtype": "f32"}
+
+
+def box_surface_ijk(n_boxes: int, resolution: int, seed: int, device) -> torch.Tensor:
+    """Faces of n random axis-aligned boxes (sides U[0.1,0.5], min corner U[0,1-side]) at resolution^3."""
+    g = torch.Generator().manual_seed(seed)
+    out = []
+    for _ in range(n_boxes):
+        side = 0.1 + 0.4 * torch.rand(3, generator=g)
+        lo = torch.rand(3, generator=g) * (1 - side)
+        a = torch.floor(lo * resolution).long()
+        b = torch.floor((lo + side) * resolution).long()
+        for axis in range(3):
+            u, v = [t for t in range(3) if t != axis]
+            gu, gv = torch.meshgrid(torch.arange(a[u], b[u] + 1), torch.arange(a[v], b[v] + 1), indexing="ij")
+            for face in (a[axis], b[axis]):
+                pts = torch.empty(gu.numel(), 3, dtype=torch.long)
+                pts[:, axis] = face
+                pts[:, u] = gu.reshape(-1)
+                pts[:, v] = gv.reshape(-1)
+                out.append(pts)
+    return torch.unique(torch.cat(out), dim=0).to(device, torch.int32)
+
+
+def leg_train(fvdb, dev, args) -> dict:
+    """conv3^3(64->64) -> ReLU -> conv3^3(64->64) on ~1M box-surface voxels at 512^3: forward +
+    dgrad + wgrad, BF16 vs the plain FP32 form; errors vs the FP64 form on the same inputs."""
+    grid = fvdb.GridBatch.from_ijk(box_surface_ijk(8, 512, 200, dev))
+    g = torch.Generator().manual_seed(201)
+    w1 = torch.randn(64, 64, 3, 3, 3, generator=g) * math.sqrt(2.0 / (27 * 64))
+    w2 = torch.randn(64, 64, 3, 3, 3, generator=g) * math.sqrt(2.0 / (27 * 64))
+    x0 = torch.randn(grid.total_voxels, 64, generator=g)
+    dy = torch.randn(grid.total_voxels, 64, generator=g)
+    pack, _ = grid.sparse_conv_kernel_map(3, 1)
+    pack.build_implicit_gemm(training=True)
+    P = int((pack.out_in_map >= 0).sum())
+    flops = 2 * 3 * 2.0 * P * 64 * 64  # two layers x (fwd, dgrad, wgrad)
+
+    def run(dtype):
+        x = x0.to(dev, dtype).requires_grad_(True)
+        a, b = w1.to(dev, dtype).requires_grad_(True), w2.to(dev, dtype).requires_grad_(True)
+        d = dy.to(dev, dtype)
+
+        def step():
+            h = torch.relu(pack.sparse_conv_3d(x, a).jdata)
+            y = pack.sparse_conv_3d(h, b).jdata
+            x.grad = a.grad = b.grad = None
+            y.backward(d)
+            return y
+
+        return step, x, a, b
+
+    res = {"voxels": grid.total_voxels, "pairs": P, "useful_flops_per_step": flops}
+    outs = {}
+    for name, dtype in (("bf16", torch.bfloat16), ("fp32", torch.float32), ("fp64", torch.float64)):
+        step, x, a, b = run(dtype)
+        if name != "fp64":
+            ms = time_ms(step, 3, 1)
+            res[name] = {"ms_per_step": ms, "tflops": flops / (ms * 1e-3) / 1e12}
+        y = step()
+        outs[name] = (y.detach(), x.grad.detach(), a.grad.detach())
+    res["bf16_vs_fp32"] = res["fp32"]["ms_per_step"] / res["bf16"]["ms_per_step"]
+    for name in ("bf16", "fp32"):
+        res[name]["errors_vs_fp64"] = {k: rel_errors(o, r) for k, o, r in zip(("y", "dx", "dw1"), outs[name], outs["fp64"])}
+    return res
+
+
+def shell_ijk(target: int, seed: int, device, res_cap: int = 4000) -> torch.Tensor:
+    """One random sphere shell voxelised at a resolution chosen to give ~target voxels."""
+    g = torch.Generator().manual_seed(seed)
+    r = 0.2 + 0.25 * float(torch.rand(1, generator=g))
+    c = 0.3 + 0.4 * torch.rand(3, generator=g)
+    R = int(min(res_cap, max(16, math.sqrt(target / (1.55 * 4 * math.pi * r * r)))))
+    d = torch.randn(int(target * 2.5), 3, generator=g)
+    p = c + r * d / d.norm(dim=1, keepdim=True)
+    ijk = torch.floor(p.clamp(0, 1 - 1e-6) * R + 0.5).to(torch.int32)
+    return torch.unique(ijk, dim=0).to(device)
+
+
+def leg_fp8(fvdb, dev, args) -> dict:
+    """~4M sphere-shell voxels at 1024^3: FP8-E4M3 3^3 conv C128->256 (per-channel scales), then
+    2^3 stride-2 transposed conv C256->128 from conv_grid(2,2) back onto the fine grid.  Timing
+    FP8 and BF16; errors vs FP64 on 4096 sampled output rows."""
+    parts = [shell_ijk(1_000_000, 300 + i, dev, 1024) for i in range(4)]
+    ijk = torch.unique(torch.cat(parts), dim=0)
+    grid = fvdb.GridBatch.from_ijk(ijk)
+    g = torch.Generator().manual_seed(301)
+    x = torch.randn(grid.total_voxels, 128, generator=g).to(dev, torch.bfloat16)
+    w1 = (torch.randn(256, 128, 3, 3, 3, generator=g) * math.sqrt(2.0 / (27 * 128))).to(dev, torch.bfloat16)
+    pack1, _ = grid.sparse_conv_kernel_map(3, 1)
+    coarse = grid.conv_grid(2, 2)
+    pack2, _ = grid.sparse_conv_kernel_map(2, 2, coarse)
+    xc = torch.randn(coarse.total_voxels, 256, generator=g).to(dev, torch.bfloat16)
+    w2 = (torch.randn(256, 128, 2, 2, 2, generator=g) * math.sqrt(2.0 / (8 * 256))).to(dev, torch.bfloat16)
+    P1 = int((pack1.out_in_map >= 0).sum())
+    P2 = int((pack2.out_in_map >= 0).sum())
+    f1, f2 = 2.0 * P1 * 128 * 256, 2.0 * P2 * 256 * 128
+    res = {"voxels": grid.total_voxels, "coarse_voxels": coarse.total_voxels, "pairs_l1": P1, "pairs_l2": P2}
+    with torch.no_grad():
+        for prec in ("fp8", "bf16"):
+            ms1 = time_ms(lambda: pack1.sparse_conv_3d(x, w1, precision=prec), 3, 1)
+            ms2 = time_ms(lambda: pack2.sparse_transpose_conv_3d(xc, w2, precision=prec), 3, 1)
+            res[prec] = {"l1_ms": ms1, "l1_tflops": f1 / (ms1 * 1e-3) / 1e12, "l2_ms": ms2, "l2_tflops": f2 / (ms2 * 1e-3) / 1e12}
+        y1 = pack1.sparse_conv_3d(x, w1, precision="fp8").jdata
+        y2 = pack2.sparse_transpose_conv_3d(xc, w2, precision="fp8").jdata
+    # FP64 reference rows through the kernel maps
+    sel = torch.randperm(grid.total_voxels, generator=g)[:4096].to(dev)
+    m1 = pack1.out_in_map[sel].long()
+    W1 = w1.double().permute(4, 3, 2, 1, 0).reshape(27, 128, 256)
+    xd = torch.cat([x.double(), torch.zeros(1, 128, dtype=torch.float64, device=dev)])
+    ref1 = torch.einsum("rkc,kco->ro", xd[torch.where(m1 >= 0, m1, grid.total_voxels)], W1)
+    mt = pack2.out_in_map_bwd[sel].long()
+    W2 = w2.double().permute(4, 3, 2, 0, 1).reshape(8, 256, 128)
+    xcd = torch.cat([xc.double(), torch.zeros(1, 256, dtype=torch.float64, device=dev)])
+    ref2 = torch.einsum("rkc,kco->ro", xcd[torch.where(mt >= 0, mt, coarse.total_voxels)], W2)
+    res["errors_vs_fp64"] = {"l1": rel_errors(y1[sel], ref1), "l2_transposed": rel_errors(y2[sel], ref2)}
+    return res
+
+
+def leg_serve(fvdb, dev, args) -> dict:
+    """Poisson arrivals, N log-uniform [1e4, 2e6] voxels per request (one sphere shell each),
+    4-layer 3^3 stack 32->64->64->32 with ReLU, BF16, continuous batching under an HBM budget;
+    against the plain FP32 per-request form on the same arrival schedule."""
+    from fvdb.serving import ContinuousBatcher, ConvStack, GPUExecutor, Request, latency_stats
+
+    rng = np.random.default_rng(400)
+    reqs = []
+    t = 0.0
+    for i in range(args.serve_requests):
+        n = int(math.exp(rng.uniform(math.log(1e4), math.log(2e6))))
+        ijk = shell_ijk(n, 400 + i, dev).cpu().pin_memory()
+        feats = torch.randn(ijk.shape[0], 32, generator=torch.Generator().manual_seed(i)).bfloat16().pin_memory()
+        t += float(rng.exponential(1.0 / args.serve_rate))
+        reqs.append((i, ijk, feats, t))
+    model = ConvStack([32, 64, 64, 32], dev, seed=0)
+    out = {"rate_per_s": args.serve_rate, "requests": len(reqs)}
+    # continuous batching (3 streams, up to 4M voxels per jagged batch) vs one request at a time in FP32
+    for name, mdl, slots, per_batch in (("bf16_batched", model, 3, None),
+                                        ("fp32_per_request", model.to_dtype(torch.float32), 1, 1)):
+        ex = GPUExecutor(mdl, dev, slots=slots)
+        srv = ContinuousBatcher(ex, hbm_budget=48 << 30, max_batch_voxels=4_000_000, slots=slots,
+                                max_batch_requests=per_batch)
+        batch = [Request(rid=i, ijk=a, features=(f if name.startswith("bf16") else f.float()), arrival=t0)
+                 for i, a, f, t0 in reqs]
+        # warm-up on the first request alone
+        srv.serve([Request(rid=-1, ijk=batch[0].ijk, features=batch[0].features, arrival=0.0)])
+        done = srv.serve(batch)
+        st = latency_stats(done)
+        st["batches"] = srv.batches
+        st["errors"] = sum(1 for r in done if r.error)
+        out[name] = st
+    return out
 
 
 def main():
@@ -360,6 +559,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / training / FP8 / serving legs")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson request rate of the serving leg (1/s)")
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving leg")
     ap.add_argument("--points", type=int, default=2_000_000,
                     help="points per grid (the headline workload uses 2M; smaller only for profiling captures)")
     args = ap.parse_args()

@@ -9,18 +9,21 @@
 // two or four kernel offsets share one 128-byte swizzle row of the A operand.  Offsets absent
 // from all 128 rows of a tile (per-tile occupancy mask) are skipped.
 //
-// Warp roles (288 threads):
+// Warp roles (320 threads):
 //   warps 0-3  gather: thread r owns row r of the tile.  Per step it issues 16-byte cp.async
 //              copies (L2 evict_last: the input features stay L2-resident while the map and
 //              output stream) of the gathered feature rows into the 128B-swizzled K-major A
-//              layout, zero-filled where the map is -1, and arrives on the stage's mbarrier when
-//              its copies land; thread 0 also fetches the stage's pre-packed weight tiles with
-//              bulk async copies.  The next tile's map row is prefetched into registers while
-//              the current tile streams.
+//              layout, zero-filled where the map is -1.  cp.async writes belong to the generic
+//              proxy, so each thread publishes a stage to the tensor core (async proxy) itself,
+//              kLag steps late: cp.async.wait_group, fence.proxy.async, then mbarrier arrive.
+//              The MMA thread therefore never fences and its MMAs stream back to back.
 //   warp 4     TMEM allocation (2 x N columns) and the single MMA-issuing thread; tile i
 //              accumulates into TMEM buffer i % 2.
-//   warps 5-8  epilogue: tcgen05.ld of the finished buffer -> scale -> BF16 -> global, then
-//              release the buffer -- overlapping the next tile's main loop.
+//   warps 5-8  epilogue: tcgen05.ld of the finished buffer -> scale -> BF16 -> a shared-memory
+//              copy of the output tile -> one bulk async store of the tile's contiguous rows;
+//              overlaps the next tile's main loop.
+//   warp 9     loader: bulk async copies of each tile's map rows (double-buffered) and of each
+//              step's pre-packed, pre-swizzled weight tiles.
 //
 // Every mbarrier wait is bounded (about a second); on expiry the CTA stops, waits for its
 // issued work, frees TMEM and raises *err = FVGB_ETIMEOUT.
@@ -42,8 +45,9 @@ using namespace tc;
 constexpr int kTileM = 128;
 constexpr int kRowBytes = 128;  // one swizzle row = 64 bf16 or 128 fp8 elements
 constexpr int kABytes = kTileM * kRowBytes;
-constexpr int kThreads = 288;
-constexpr int kMaxMapRegs = 32;
+constexpr int kThreads = 320;  // 4 gather + 1 MMA + 4 epilogue + 1 loader warps
+constexpr int kMaxMapStage = 32;  // map tiles staged in shared memory up to K = 32
+constexpr int kLag = 2;  // cp.async groups a gather thread keeps in flight before publishing a stage
 
 struct FwdArgs {
     const uint8_t *x;
@@ -65,6 +69,7 @@ struct FwdArgs {
     int32_t *err;
     int32_t stages;
     int64_t n_tiles;
+    int32_t direct_store;  // 1: output rows contiguous (ldy == cout, cout % 8 == 0): one bulk store per tile
 };
 
 struct Steps {
@@ -73,12 +78,17 @@ struct Steps {
     int n_steps;
 };
 
-__device__ __forceinline__ Steps tile_steps(const FwdArgs &a, int64_t tile) {
+__device__ __forceinline__ uint32_t load_mask(const FwdArgs &a, int64_t tile) {
+    if (a.K > 32) return 0;
+    const uint32_t all = a.K == 32 ? 0xffffffffu : ((1u << a.K) - 1u);
+    return a.tile_mask ? (__ldg(a.tile_mask + tile) & all) : all;
+}
+
+__device__ __forceinline__ Steps make_steps(const FwdArgs &a, uint32_t mask) {
     Steps s;
     if (a.K <= 32) {
-        const uint32_t all = a.K == 32 ? 0xffffffffu : ((1u << a.K) - 1u);
-        s.kbits = a.tile_mask ? (a.tile_mask[tile] & all) : all;
-        s.n_act = __popc(s.kbits);
+        s.kbits = mask;
+        s.n_act = __popc(mask);
     } else {
         s.kbits = 0;
         s.n_act = a.K;
@@ -125,24 +135,30 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
     constexpr int kBTile = BN * kRowBytes;
     const int S = a.stages;
     const int kStage = kABytes + a.pack * kBTile;
-    const bool stage_map = a.K <= kMaxMapRegs;
+    const bool stage_map = a.K <= kMaxMapStage;
+    const int map_words = stage_map ? kTileM * a.K : 0;  // per buffer; 512*K bytes, 16-byte aligned
     int32_t *map_sm = reinterpret_cast<int32_t *>(smem + S * kStage);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(map_sm + (stage_map ? kTileM * a.K : 0));
-    uint64_t *full = bars, *empty = bars + S, *tfull = bars + 2 * S, *tempty = tfull + 2, *fin = tempty + 2;
+    uint8_t *ystage = reinterpret_cast<uint8_t *>(map_sm + 2 * map_words);  // [128 rows x cout] bf16
+    uint64_t *bars = reinterpret_cast<uint64_t *>(ystage + (a.direct_store ? kTileM * BN * 2 : 0));
+    uint64_t *full = bars, *empty = bars + S, *tfull = bars + 2 * S, *tempty = tfull + 2, *mfull = tempty + 2,
+             *mempty = mfull + 2, *fin = mempty + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
     volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr uint32_t kTmemCols = 2 * BN;
+    const int64_t stride = gridDim.x;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full[s], kTileM + 1);
+            mbar_init(&full[s], kTileM + 1);  // 128 gather threads + the loader's expect_tx
             mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&tfull[b], 1);
             mbar_init(&tempty[b], kTileM);
+            mbar_init(&mfull[b], 1);
+            mbar_init(&mempty[b], kTileM);
         }
         mbar_init(fin, 1);
         *abort = 0;
@@ -154,85 +170,78 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
     const uint32_t tmem = *tmem_slot;
 
     if (warp < 4) {
-        // ----------------------------------------------------------------- gather producer
+        // ----------------------------------------------------------------- gather (A operand)
         const int r = threadIdx.x;
-        const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
-        int32_t pre[kMaxMapRegs];
+        const uint64_t keep = policy_evict_last();
+        uint32_t it = 0, sig = 0;
         int64_t tile = blockIdx.x;
-        if (stage_map && tile < a.n_tiles) {
-#pragma unroll
-            for (int k = 0; k < kMaxMapRegs; ++k)
-                if (k < a.K) pre[k] = ld_nc_hint(a.map + (tile * kTileM + r) * a.K + k, stream);
-        }
-        uint32_t it = 0;
-        for (; tile < a.n_tiles && !*abort; tile += gridDim.x) {
+        uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
+        for (int i = 0; tile < a.n_tiles && !*abort; tile += stride, ++i) {
+            const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
             const int64_t row = tile * kTileM + r;
-            if (stage_map) {
-                // own row only: no cross-thread synchronisation needed
-#pragma unroll
-                for (int k = 0; k < kMaxMapRegs; ++k)
-                    if (k < a.K) map_sm[r * a.K + k] = (pre[k] >= 0 && pre[k] < a.n_x) ? pre[k] : -1;
-                const int64_t nxt = tile + gridDim.x;
-                if (nxt < a.n_tiles) {
-#pragma unroll
-                    for (int k = 0; k < kMaxMapRegs; ++k)
-                        if (k < a.K) pre[k] = ld_nc_hint(a.map + (nxt * kTileM + r) * a.K + k, stream);
-                }
-            }
-            const Steps st = tile_steps(a, tile);
+            const int mb = i & 1;
+            if (stage_map && !mbar_wait(&mfull[mb], (i >> 1) & 1, abort)) break;
+            const int32_t *mrow = map_sm + mb * map_words + r * a.K;
+            const Steps st = make_steps(a, mask_cur);
             StepWalker w{st.kbits, 0, 0, -1};
-            for (int s = 0; s < st.n_steps; ++s, ++it) {
+            bool ok = true;
+            for (int s = 0; s < st.n_steps; ++s) {
                 int ks[4], c;
                 w.next(a, ks, c);
                 const int stage = it % S;
-                if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) break;
+                if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) {
+                    ok = false;
+                    break;
+                }
                 const uint32_t As = smem_u32(smem + stage * kStage);
-                int nb = 0;
 #pragma unroll
                 for (int p = 0; p < 4; ++p) {
                     if (p >= a.pack || ks[p] < 0) continue;
-                    ++nb;
                     int32_t src;
                     if (stage_map) {
-                        src = map_sm[r * a.K + ks[p]];
+                        src = mrow[ks[p]];
                     } else {
                         src = row < a.n_out ? a.map[row * a.K + ks[p]] : -1;
-                        if (src >= a.n_x) src = -1;
                     }
+                    if (src >= a.n_x) src = -1;
                     const uint8_t *g = a.x + (src >= 0 ? (int64_t)src * a.ldx_bytes + (int64_t)c * kRowBytes : 0);
                     const int bytes = min(kRowBytes, a.row_bytes - c * kRowBytes);
                     const int j0 = p * (a.row_bytes >> 4);
                     for (int j = 0; j < (bytes >> 4); ++j)
                         cp_async_16_hint(As + sw128_offset(r, j0 + j), g + j * 16, src >= 0 ? 16u : 0u, keep);
                 }
-                cp_async_arrive_noinc(&full[stage]);
-                if (r == 0) {
-                    mbar_arrive_expect_tx(&full[stage], nb * kBTile);
-                    int q = 0;
-#pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        if (p >= a.pack || ks[p] < 0) continue;
-                        bulk_g2s(As + kABytes + q * kBTile,
-                                 a.wpack + ((int64_t)ks[p] * a.nchunks + c) * kBTile, kBTile, &full[stage]);
-                        ++q;
-                    }
+                cp_async_commit();
+                ++it;
+                if (it - sig > kLag) {
+                    // the copies of step `sig` have landed: publish them to the async proxy (tcgen05.mma)
+                    cp_async_wait_group<kLag>();
+                    fence_proxy_async();
+                    mbar_arrive(&full[sig % S]);
+                    ++sig;
                 }
             }
+            if (stage_map) mbar_arrive(&mempty[mb]);
+            if (!ok) break;
+            mask_cur = mask_next;
         }
-        cp_async_wait_all();
+        cp_async_wait_group<0>();
+        fence_proxy_async();
+        for (; sig < it; ++sig) mbar_arrive(&full[sig % S]);
     } else if (warp == 4) {
         // ----------------------------------------------------------------- MMA issuer
         if (lane == 0) {
             constexpr uint32_t idesc = EBYTES == 2 ? idesc_m128(BN, 1, 1) : idesc_m128(BN, 0, 0);
             uint32_t it = 0;
-            int i = 0;
             bool ok = true;
-            for (int64_t tile = blockIdx.x; tile < a.n_tiles && ok; tile += gridDim.x, ++i) {
+            int64_t tile = blockIdx.x;
+            uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
+            for (int i = 0; tile < a.n_tiles && ok; tile += stride, ++i) {
+                const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
                 const int b = i & 1;
                 if (!mbar_wait(&tempty[b], ((i >> 1) & 1) ^ 1, abort)) break;
                 tc_fence_after();
                 const uint32_t d = tmem + b * BN;
-                const Steps st = tile_steps(a, tile);
+                const Steps st = make_steps(a, mask_cur);
                 StepWalker w{st.kbits, 0, 0, -1};
                 uint32_t acc = 0;
                 for (int s = 0; s < st.n_steps; ++s, ++it) {
@@ -243,7 +252,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                         ok = false;
                         break;
                     }
-                    fence_proxy_async();
                     tc_fence_after();
                     const uint32_t As = smem_u32(smem + stage * kStage);
                     const int bytes = min(kRowBytes, a.row_bytes - c * kRowBytes);
@@ -269,6 +277,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                     mma_commit(&tfull[b]);
                 else
                     mbar_arrive(&tfull[b]);
+                mask_cur = mask_next;
             }
             // all issued MMAs complete before TMEM is released
             mma_commit(fin);
@@ -277,19 +286,28 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
             }
         }
         __syncwarp();
-    } else {
+    } else if (warp < 9) {
         // ----------------------------------------------------------------- epilogue
-        const int q4 = warp & 3;  // TMEM lane quarter this warp may access
-        int i = 0;
-        for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++i) {
+        const int et = threadIdx.x - 160;  // 0..127
+        const int q4 = warp & 3;           // TMEM lane quarter this warp may access
+        const int rt = q4 * 32 + lane;     // row of the tile this thread drains
+        int64_t tile = blockIdx.x;
+        uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
+        for (int i = 0; tile < a.n_tiles; tile += stride, ++i) {
+            const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
             const int b = i & 1;
             const bool ready = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (i >> 1) & 1, abort) && !*abort);
             if (!ready) break;
             tc_fence_after();
-            const Steps st = tile_steps(a, tile);
-            const int64_t row = tile * kTileM + q4 * 32 + lane;
+            const Steps st = make_steps(a, mask_cur);
+            const int64_t m0 = tile * kTileM;
+            const int64_t left = a.n_out - m0;
+            const int rows = left < kTileM ? (int)left : kTileM;
             const uint32_t tbase = tmem + b * BN + ((uint32_t)(q4 * 32) << 16);
-            __nv_bfloat16 *yrow = reinterpret_cast<__nv_bfloat16 *>(a.y) + row * a.ldy;
+            if (a.direct_store) {
+                if (et == 0) bulk_wait_read<0>();  // the staging tile of the previous store has been read
+                named_barrier(1, kTileM);
+            }
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 float v[16];
@@ -299,30 +317,93 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
 #pragma unroll
                     for (int t = 0; t < 16; ++t) v[t] = 0.f;
                 }
-                if (row >= a.n_out) continue;
-                if (c0 + 16 <= a.cout) {
-                    uint32_t packed[8];
+                if (rt >= rows || c0 >= a.cout) continue;
+                uint32_t packed[8];
 #pragma unroll
-                    for (int t = 0; t < 8; ++t) {
-                        float lo = v[2 * t], hi = v[2 * t + 1];
-                        if (a.scale) {
-                            lo *= a.scale[c0 + 2 * t];
-                            hi *= a.scale[c0 + 2 * t + 1];
-                        }
-                        __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
-                        packed[t] = *reinterpret_cast<uint32_t *>(&h);
+                for (int t = 0; t < 8; ++t) {
+                    const int cc = c0 + 2 * t;
+                    float lo = v[2 * t], hi = v[2 * t + 1];
+                    if (a.scale) {
+                        lo *= cc < a.cout ? a.scale[cc] : 0.f;
+                        hi *= cc + 1 < a.cout ? a.scale[cc + 1] : 0.f;
                     }
-                    uint4 *dst = reinterpret_cast<uint4 *>(yrow + c0);
+                    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+                    packed[t] = *reinterpret_cast<uint32_t *>(&h);
+                }
+                if (a.direct_store) {
+                    // cout % 8 == 0: whole 16-byte groups; the last group of a 16-wide block may be cut
+                    uint4 *dst = reinterpret_cast<uint4 *>(ystage + ((size_t)rt * a.cout + c0) * 2);
                     dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                    if (c0 + 8 < a.cout) dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                 } else {
-                    for (int t = 0; t < 16 && c0 + t < a.cout; ++t)
-                        yrow[c0 + t] = __float2bfloat16_rn(a.scale ? v[t] * a.scale[c0 + t] : v[t]);
+                    __nv_bfloat16 *yrow = reinterpret_cast<__nv_bfloat16 *>(a.y) + (m0 + rt) * a.ldy;
+                    const __nv_bfloat16 *hv = reinterpret_cast<const __nv_bfloat16 *>(packed);
+                    for (int t = 0; t < 16 && c0 + t < a.cout; ++t) yrow[c0 + t] = hv[t];
                 }
             }
             tc_fence_before();
             mbar_arrive(&tempty[b]);
+            if (a.direct_store) {
+                fence_proxy_async();  // staging writes -> visible to the bulk store (async proxy)
+                named_barrier(1, kTileM);
+                if (et == 0) {
+                    bulk_s2g(a.y + m0 * a.ldy * 2, smem_u32(ystage), (uint32_t)(rows * a.cout * 2));
+                    bulk_commit();
+                }
+            }
+            mask_cur = mask_next;
         }
+        if (a.direct_store && et == 0) bulk_wait<0>();
+    } else {
+        // ----------------------------------------------------------------- loader (bulk copies)
+        if (lane == 0) {
+            uint32_t it = 0;
+            int64_t tile = blockIdx.x;
+            const uint32_t map_bytes = (uint32_t)map_words * 4;
+            if (stage_map && tile < a.n_tiles) {
+                mbar_arrive_expect_tx(&mfull[0], map_bytes);
+                bulk_g2s(smem_u32(map_sm), a.map + tile * kTileM * a.K, map_bytes, &mfull[0]);
+            }
+            uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
+            for (int i = 0; tile < a.n_tiles && !*abort; tile += stride, ++i) {
+                const int64_t nxt = tile + stride;
+                const uint32_t mask_next = nxt < a.n_tiles ? load_mask(a, nxt) : 0;
+                if (stage_map && nxt < a.n_tiles) {
+                    const int nb = (i + 1) & 1;
+                    if (!mbar_wait(&mempty[nb], (((i + 1) >> 1) & 1) ^ 1, abort)) break;
+                    mbar_arrive_expect_tx(&mfull[nb], map_bytes);
+                    bulk_g2s(smem_u32(map_sm + nb * map_words), a.map + nxt * kTileM * a.K, map_bytes, &mfull[nb]);
+                }
+                const Steps st = make_steps(a, mask_cur);
+                StepWalker w{st.kbits, 0, 0, -1};
+                bool ok = true;
+                for (int s = 0; s < st.n_steps; ++s, ++it) {
+                    int ks[4], c;
+                    w.next(a, ks, c);
+                    const int stage = it % S;
+                    if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    int nb = 0;
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) nb += (p < a.pack && ks[p] >= 0) ? 1 : 0;
+                    mbar_arrive_expect_tx(&full[stage], nb * kBTile);
+                    const uint32_t Bs = smem_u32(smem + stage * kStage) + kABytes;
+                    int q = 0;
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        if (p >= a.pack || ks[p] < 0) continue;
+                        bulk_g2s(Bs + q * kBTile, a.wpack + ((int64_t)ks[p] * a.nchunks + c) * kBTile, kBTile,
+                                 &full[stage]);
+                        ++q;
+                    }
+                }
+                if (!ok) break;
+                mask_cur = mask_next;
+            }
+        }
+        __syncwarp();
     }
     tc_fence_before();
     __syncthreads();
@@ -386,10 +467,13 @@ int sm_count() {
 template <int BN, int EB>
 int launch_fwd(FwdArgs a, cudaStream_t s) {
     const int stage = kABytes + a.pack * BN * kRowBytes;
-    const int map_bytes = a.K <= kMaxMapRegs ? kTileM * a.K * 4 : 0;
-    const int fixed = 1024 + map_bytes + (2 * 8 + 5) * 8 + 16;
+    const int map_bytes = a.K <= kMaxMapStage ? 2 * kTileM * a.K * 4 : 0;
+    a.direct_store = (a.direct_store && BN <= 128) ? 1 : 0;  // staging tile only where it fits
+    const int fixed = 1024 + map_bytes + (a.direct_store ? kTileM * BN * 2 : 0) + (2 * 8 + 9) * 8 + 16;
     int stages = 8;
-    while (stages > 2 && stages * stage + fixed > 227 * 1024) --stages;
+    while (stages > kLag + 1 && stages * stage + fixed > 227 * 1024) --stages;
+    // a gather thread publishes a stage kLag steps late, so the ring needs more than kLag stages
+    if (stages < kLag + 1 || stages * stage + fixed > 227 * 1024) return FVGB_EINVAL;
     a.stages = stages;
     const int smem = stages * stage + fixed;
     auto kern = conv_tc_fwd_kernel<BN, EB>;
@@ -474,6 +558,7 @@ extern "C" int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32
     a.err = err_dev;
     a.stages = 0;
     a.n_tiles = ceil_div(n_out, kTileM);
+    a.direct_store = (ldy == c_out && c_out % 8 == 0) ? 1 : 0;
     cudaStream_t s = as_stream(stream);
     if (eb == 2) {
         switch (BN) {

@@ -32,6 +32,7 @@ struct KmapParams {
     int32_t *nbsizes;
     uint32_t *tile_mask;    // OR of row occupancy per 128-row tile (K <= 32), may be null
     int32_t window;         // source leaves staged per CTA (0: not staged)
+    int32_t disp_table;     // 1: per-offset displacements tabulated in shared memory
 };
 
 struct WinLeaf {
@@ -44,7 +45,7 @@ __device__ inline uint32_t win_prefix(const WinLeaf &w, uint32_t word) {
     return (w.prefix[word >> 1] >> ((word & 1) * 16)) & 0xffffu;
 }
 
-// Shared memory: WinLeaf[window] | uint16 slots[512] | int32 counts[K] | uint32 tmask[8]
+// Shared memory: WinLeaf[window] | uint16 slots[512] | int32 counts[K] | uint32 tmask[8] | int32 disp[K]
 __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
     extern __shared__ __align__(16) uint8_t kmap_smem[];
     WinLeaf *win = reinterpret_cast<WinLeaf *>(kmap_smem);
@@ -52,6 +53,8 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
     int32_t *counts = reinterpret_cast<int32_t *>(slots + 512);
     const int nk_smem = p.nbsizes ? min(p.K, kMaxKSmem) : 0;
     uint32_t *tmask = reinterpret_cast<uint32_t *>(counts + nk_smem);
+    // per-offset displacement (dx, dy, dz), 10 bits each biased by 512 (kernel extents <= 511)
+    int32_t *kdisp = p.disp_table ? reinterpret_cast<int32_t *>(tmask + 8) : nullptr;
     __shared__ int32_t s_count;
 
     const int64_t leaf_id = blockIdx.x;
@@ -70,6 +73,11 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
 
     if (threadIdx.x == 0) s_count = 0;
     if (threadIdx.x < 8) tmask[threadIdx.x] = 0;
+    if (kdisp)
+        for (int k = threadIdx.x; k < p.K; k += blockDim.x) {
+            const int32_t i2 = k / (p.K0 * p.K1), i1 = (k / p.K0) % p.K1, i0 = k % p.K0;
+            kdisp[k] = ((p.st2 + i2 + 512) << 20) | ((p.st1 + i1 + 512) << 10) | (p.st0 + i0 + 512);
+        }
     for (int k = threadIdx.x; k < nk_smem; k += blockDim.x) counts[k] = 0;
     if (staged) {
         for (int w = threadIdx.x; w < W; w += blockDim.x) {
@@ -101,18 +109,29 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
     __syncthreads();
 
     const int32_t cnt = s_count;
-    const int64_t total = (int64_t)cnt * p.K;
-    const int32_t K01 = p.K0 * p.K1;
+    const int32_t total = cnt * p.K;
     const int64_t t0 = tbase >> 7;  // first 128-row tile this leaf's rows touch
-    for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
-        const int32_t r = (int32_t)(e / p.K), k = (int32_t)(e - (int64_t)r * p.K);
+    // (row, offset) of entry e = threadIdx.x + j * blockDim.x, advanced without divisions
+    const int32_t dr = blockDim.x / p.K, dk = blockDim.x % p.K;
+    int32_t r = threadIdx.x / p.K, k = threadIdx.x % p.K;
+    int64_t my_tile = -1;
+    uint32_t my_bits = 0;
+    for (int32_t e = threadIdx.x; e < total; e += blockDim.x) {
         const uint32_t s = slots[r];
         const int32_t tx = ox + (int32_t)(s >> 6), ty = oy + (int32_t)((s >> 3) & 7), tz = oz + (int32_t)(s & 7);
-        // kIdx = (i2*K1 + i1)*K0 + i0 with i2 offsetting x (extent k2) and i0 offsetting z
-        const int32_t i2 = k / K01, i1 = (k / p.K0) % p.K1, i0 = k % p.K0;
-        const int32_t sx = tx * p.S2 + p.st2 + i2;
-        const int32_t sy = ty * p.S1 + p.st1 + i1;
-        const int32_t sz = tz * p.S0 + p.st0 + i0;
+        int32_t dx, dy, dz;
+        if (kdisp) {
+            const int32_t d = kdisp[k];
+            dx = (d >> 20) - 512;
+            dy = ((d >> 10) & 1023) - 512;
+            dz = (d & 1023) - 512;
+        } else {
+            // kIdx = (i2*K1 + i1)*K0 + i0 with i2 offsetting x (extent k2) and i0 offsetting z
+            dx = p.st2 + k / (p.K0 * p.K1);
+            dy = p.st1 + (k / p.K0) % p.K1;
+            dz = p.st0 + k % p.K0;
+        }
+        const int32_t sx = tx * p.S2 + dx, sy = ty * p.S1 + dy, sz = tz * p.S0 + dz;
         int64_t idx = -1;
         if (staged) {
             const int32_t w = (((sx >> 3) - lx0) * wy + ((sy >> 3) - ly0)) * wz + ((sz >> 3) - lz0);
@@ -134,9 +153,24 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
                 if (k < kMaxKSmem) atomicAdd(&counts[k], 1);
                 else atomicAdd(p.nbsizes + k, 1);
             }
-            if (p.tile_mask) atomicOr(&tmask[((tbase + r) >> 7) - t0], 1u << k);
+            if (p.tile_mask) {
+                const int64_t t = (tbase + r) >> 7;
+                if (t != my_tile) {
+                    if (my_bits) atomicOr(&tmask[my_tile - t0], my_bits);
+                    my_tile = t;
+                    my_bits = 0;
+                }
+                my_bits |= 1u << k;
+            }
+        }
+        k += dk;
+        r += dr;
+        if (k >= p.K) {
+            k -= p.K;
+            ++r;
         }
     }
+    if (my_bits) atomicOr(&tmask[my_tile - t0], my_bits);
     if (p.nbsizes || p.tile_mask) {
         __syncthreads();
         for (int k = threadIdx.x; k < nk_smem; k += blockDim.x)
@@ -263,7 +297,9 @@ extern "C" int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const i
     const int64_t W = (int64_t)span(p.S2, p.st2, p.K2) * span(p.S1, p.st1, p.K1) * span(p.S0, p.st0, p.K0);
     p.window = W <= kMaxWindow ? (int32_t)W : 0;
     const int nk_smem = nbsizes ? (int)std::min<int64_t>(K, kMaxKSmem) : 0;
-    const size_t smem = (size_t)p.window * sizeof(WinLeaf) + 512 * sizeof(uint16_t) + nk_smem * 4 + 8 * 4;
+    p.disp_table = (K <= kMaxKSmem && ksize[0] <= 511 && ksize[1] <= 511 && ksize[2] <= 511) ? 1 : 0;
+    const size_t smem = (size_t)p.window * sizeof(WinLeaf) + 512 * sizeof(uint16_t) + nk_smem * 4 + 8 * 4 +
+                        (p.disp_table ? (size_t)K * 4 : 0);
     kmap_leaf_kernel<<<(unsigned)tgt->num_leaves, kKmapThreads, smem, as_stream(stream)>>>(p);
     count_launches(1);
     return launch_status();

@@ -79,12 +79,13 @@ class ContinuousBatcher:
     (one CUDA stream each)."""
 
     def __init__(self, executor: Executor, hbm_budget: int, max_batch_voxels: int, slots: int = 2,
-                 clock: Callable[[], float] = time.perf_counter):
+                 clock: Callable[[], float] = time.perf_counter, max_batch_requests: int | None = None):
         if slots < 1:
             raise ValueError("slots must be >= 1")
         self.ex = executor
         self.budget = int(hbm_budget)
         self.max_batch_voxels = int(max_batch_voxels)
+        self.max_batch_requests = max_batch_requests
         self.slots = slots
         self.clock = clock
         self.queue: collections.deque[Request] = collections.deque()
@@ -138,6 +139,8 @@ class ContinuousBatcher:
         while free and self.queue:
             batch, vox, nbytes = [], 0, 0
             while self.queue:
+                if self.max_batch_requests is not None and len(batch) >= self.max_batch_requests:
+                    break
                 r = self.queue[0]
                 need = self.ex.footprint(r)
                 if self.used + nbytes + need > self.budget or vox + r.n_voxels > self.max_batch_voxels:

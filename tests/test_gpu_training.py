@@ -66,8 +66,8 @@ def _stack(fvdb, dev, dtype, seed=0, recompute=False):
 def test_finite_differences_fp64_and_bf16_gradients(cuda_device):
     """conv3^3(64->64) -> ReLU -> conv3^3(64->64) on a box-surface grid: analytic FP64 gradients
     of L = <y, dy> against FP64 central differences (eps = 1e-4) on 64 random features and 64
-    random weights (rel error <= 1e-5 each, |g| > 1e-3), then the BF16 gradients against the
-    FP64 ones (rel-L2 <= 1e-2)."""
+    random second-layer weights (error <= 1e-5 of max(|g|, 1e-3) each), then the BF16
+    gradients against the FP64 ones (rel-L2 <= 1e-2)."""
     import fvdb
 
     from tests.synth import box_surfaces
@@ -94,7 +94,13 @@ def test_finite_differences_fp64_and_bf16_gradients(cuda_device):
             fd = (loss(xp) - loss(xm)).item() / (2 * eps)
             an = gx[i, j].item()
             assert abs(fd - an) <= 1e-5 * max(abs(an), 1e-3) + 1e-7
-        wdat = c1.weight.data  # (Do, Di, K0, K1, K2) view of (K2, K1, K0, Di, Do) storage
+        # Weights: the second layer's (the loss is linear in them through the whole stack).  A
+        # first-layer weight moves ~all pre-activations of one channel, so about one ReLU kink is
+        # crossed per 1e-4 perturbation and central differences are not valid there; the
+        # first-layer gradient is checked exactly against the reference gradient instead
+        # (test_gradient_matches_reference_autograd).
+        gw2 = c2.weight.grad.clone()
+        wdat = c2.weight.data  # (Do, Di, K0, K1, K2) view of (K2, K1, K0, Di, Do) storage
         for _ in range(64):
             e = tuple(int(v) for v in np.unravel_index(int(rng.integers(wdat.numel())), tuple(wdat.shape)))
             old = wdat[e].item()
@@ -104,7 +110,7 @@ def test_finite_differences_fp64_and_bf16_gradients(cuda_device):
             lm = loss(x).item()
             wdat[e] = old
             fd = (lp - lm) / (2 * eps)
-            an = gw1[e].item()
+            an = gw2[e].item()
             assert abs(fd - an) <= 1e-5 * max(abs(an), 1e-3) + 1e-7
     # BF16 stack with the same weights
     net16, d1, d2 = _stack(fvdb, cuda_device, torch.bfloat16)

@@ -49,7 +49,7 @@ def _req(rid, n, arrival=0.0):
 def test_budget_admission_and_continuous_batching():
     ex = FakeExecutor()
     srv = ContinuousBatcher(ex, hbm_budget=10 * 3000, max_batch_voxels=2000, slots=2)
-    reqs = [_req(i, 1000, arrival=0.002 * i) for i in range(12)]
+    reqs = [_req(i, 1000, arrival=0.004 * (i // 3)) for i in range(12)]  # arrivals in bursts of three
     out = srv.serve(reqs)
     assert all(r.error is None for r in out)
     assert all(torch.equal(r.output, r.features * 2) for r in out)
