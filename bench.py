@@ -461,6 +461,22 @@ def leg_train(fvdb, dev, args) -> dict:
     res["bf16_vs_fp32"] = res["fp32"]["ms_per_step"] / res["bf16"]["ms_per_step"]
     for name in ("bf16", "fp32"):
         res[name]["errors_vs_fp64"] = {k: rel_errors(o, r) for k, o, r in zip(("y", "dx", "dw1"), outs[name], outs["fp64"])}
+    # BF16 kernels against FP64 arithmetic on the same BF16-rounded operands and activations (same
+    # ReLU masks): separates what the kernels add from BF16 storage (whose rounding of layer-1
+    # outputs flips ReLU masks near zero and dominates the end-to-end gradient error above).
+    bf = lambda t: t.bfloat16().double()
+    xq = x0.to(dev).bfloat16().double().requires_grad_(True)
+    w1q = w1.to(dev).bfloat16().double().requires_grad_(True)
+    w2q = w2.to(dev).bfloat16().double()
+    pre = pack.sparse_conv_3d(xq, w1q).jdata
+    y1 = bf(pre.detach())
+    h = torch.relu(y1).requires_grad_(True)
+    y2 = pack.sparse_conv_3d(h, w2q).jdata
+    dh = bf(torch.autograd.grad(y2, h, bf(dy.to(dev)))[0]) * (y1 > 0)
+    dxq, dw1q = torch.autograd.grad(pre, (xq, w1q), dh)
+    res["bf16"]["errors_vs_fp64_same_rounding"] = {
+        "y": rel_errors(outs["bf16"][0], bf(y2.detach())), "dx": rel_errors(outs["bf16"][1], bf(dxq)),
+        "dw1": rel_errors(outs["bf16"][2], bf(dw1q))}
     return res
 
 
@@ -491,6 +507,8 @@ def leg_fp8(fvdb, dev, args) -> dict:
     pack2, _ = grid.sparse_conv_kernel_map(2, 2, coarse)
     xc = torch.randn(coarse.total_voxels, 256, generator=g).to(dev, torch.bfloat16)
     w2 = (torch.randn(256, 128, 2, 2, 2, generator=g) * math.sqrt(2.0 / (8 * 256))).to(dev, torch.bfloat16)
+    pack1.build_implicit_gemm()
+    pack2.build_implicit_gemm(training=True)  # forward map + the transposed map the transposed conv reads
     P1 = int((pack1.out_in_map >= 0).sum())
     P2 = int((pack2.out_in_map >= 0).sum())
     f1, f2 = 2.0 * P1 * 128 * 256, 2.0 * P2 * 256 * 128

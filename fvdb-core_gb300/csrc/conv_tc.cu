@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full[s], kTileM + 1);
+            mbar_init(&full[s], kTileM);  // one arrival per gather thread
             mbar_init(&empty[s], 1);
         }
         mbar_init(accum, 1);
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
     int steps = 0;  // active stages: the gather warps run the same loop as the MMA thread
     if (warp < 4) {
         const int r = threadIdx.x;
-        int it = 0;
+        int it = 0, sig = 0;
         for (int64_t t = 0; t < n_tiles; ++t)
             if (tile_active(t)) ++steps;
         for (int64_t t = 0; t < n_tiles && !*abort; ++t) {
@@ -188,11 +188,20 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
                 for (int e = 0; e < a.cin; e += 8)
                     cp_async_16(base + mn_offset(r, j * a.cin + e), xrow + e * 2, src >= 0 ? 16u : 0u);
             }
-            cp_async_arrive_noinc(&full[stage]);
-            if (r == 0) mbar_arrive(&full[stage]);
+            // cp.async writes are generic-proxy writes: each thread publishes a stage to the
+            // tensor core (async proxy) itself, one step late, so the MMA thread never fences
+            cp_async_commit();
             ++it;
+            if (it - sig > 1) {
+                cp_async_wait_group<1>();
+                fence_proxy_async();
+                mbar_arrive(&full[sig % S]);
+                ++sig;
+            }
         }
-        cp_async_wait_all();
+        cp_async_wait_group<0>();
+        fence_proxy_async();
+        for (; sig < it; ++sig) mbar_arrive(&full[sig % S]);
     } else if (warp == 4 && lane == 0) {
         constexpr uint32_t idesc = idesc_m128(BN, 1, 1) | (1u << 15) | (1u << 16);  // bf16, A and B MN-major
         int it = 0;
@@ -200,7 +209,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
             if (!tile_active(t)) continue;
             const int stage = it % S;
             if (!mbar_wait(&full[stage], (it / S) & 1, abort)) break;
-            fence_proxy_async();
             tc_fence_after();
             const uint32_t As = smem_u32(smem + stage * kStage), Bs = As + kBOff;
 #pragma unroll

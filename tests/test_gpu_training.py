@@ -120,8 +120,28 @@ def test_finite_differences_fp64_and_bf16_gradients(cuda_device):
     x16 = x.bfloat16().requires_grad_(True)
     y16 = net16(fvdb.nn.VDBTensor(grid, grid.jagged_like(x16))).data.jdata
     (y16.float() * dy.float()).sum().backward()
-    assert rel_l2(x16.grad.double().cpu().numpy(), gx.cpu().numpy()) <= 1e-2
-    assert rel_l2(d1.weight.grad.double().cpu().numpy(), gw1.cpu().numpy()) <= 1e-2
+    # (a) against FP64 end to end.  BF16 rounding of the first layer's output flips the ReLU mask
+    #     of the ~0.2 % of pre-activations within rounding distance of zero, and each flip drops or
+    #     adds a whole gradient term: ~4 % rel-L2 on dx and dW1 (the same 3.9 % comes out of a CPU
+    #     emulation of BF16 storage with the FP64 oracle), so the bound here is 6e-2.
+    assert rel_l2(y16.double().cpu().numpy(), net(fvdb.nn.VDBTensor(grid, grid.jagged_like(x))).data.jdata.detach().cpu().numpy()) <= 1e-2
+    assert rel_l2(x16.grad.double().cpu().numpy(), gx.cpu().numpy()) <= 6e-2
+    assert rel_l2(d1.weight.grad.double().cpu().numpy(), gw1.cpu().numpy()) <= 6e-2
+    # (b) against FP64 arithmetic on the same BF16-rounded operands and activations (same masks):
+    #     what the BF16 kernels add beyond BF16 storage must stay within 1e-2.
+    bf = lambda t: t.bfloat16().double()
+    pack, _ = grid.sparse_conv_kernel_map(3, 1)
+    xq = x16.detach().double().requires_grad_(True)
+    w1q = d1.weight.detach().double().requires_grad_(True)
+    w2q = d2.weight.detach().double()
+    pre = pack.sparse_conv_3d(xq, w1q).jdata
+    y1 = bf(pre.detach())
+    h = torch.relu(y1).requires_grad_(True)
+    dh = torch.autograd.grad(pack.sparse_conv_3d(h, w2q).jdata, h, bf(dy))[0]
+    dh = bf(dh) * (y1 > 0)
+    dxq, dw1q = torch.autograd.grad(pre, (xq, w1q), dh)
+    assert rel_l2(x16.grad.double().cpu().numpy(), bf(dxq).cpu().numpy()) <= 1e-2
+    assert rel_l2(d1.weight.grad.double().cpu().numpy(), bf(dw1q).cpu().numpy()) <= 1e-2
 
 
 def test_gradient_matches_reference_autograd(cuda_device):
