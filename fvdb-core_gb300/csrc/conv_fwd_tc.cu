@@ -9,20 +9,23 @@
 // two or four kernel offsets share one 128-byte swizzle row of the A operand.  Offsets absent
 // from all 128 rows of a tile (per-tile occupancy mask) are skipped.
 //
-// Warp roles (320 threads):
-//   warps 0-3  gather: thread r owns row r of the tile.  Per step it issues 16-byte cp.async
-//              copies (L2 evict_last: the input features stay L2-resident while the map and
-//              output stream) of the gathered feature rows into the 128B-swizzled K-major A
-//              layout, zero-filled where the map is -1.  cp.async writes belong to the generic
-//              proxy, so each thread publishes a stage to the tensor core (async proxy) itself,
-//              kLag steps late: cp.async.wait_group, fence.proxy.async, then mbarrier arrive.
-//              The MMA thread therefore never fences and its MMAs stream back to back.
-//   warp 4     TMEM allocation (2 x N columns) and the single MMA-issuing thread; tile i
+// Warp roles (448 threads):
+//   warps 0-7  gather: each warp fills 16 rows of the A tile.  Lane l copies 16-byte chunk l%8 of
+//              rows l/8, l/8+4, l/8+8, l/8+12, so one warp instruction moves four whole 128-byte
+//              A rows (per-SM cp.async throughput is set by the number of issuing warps and the
+//              distinct lines per instruction, not by bytes).  Copies are 16-byte cp.async (L2
+//              evict_last: the input features stay L2-resident while the map and output stream)
+//              into the 128B-swizzled K-major A layout; absent entries (map -1) are zero-stored
+//              with st.shared.  Both are generic-proxy writes, so each warp publishes a stage to
+//              the tensor core (async proxy) itself, kLag steps late: cp.async.wait_group,
+//              fence.proxy.async, __syncwarp, one mbarrier arrive.  The MMA thread never fences
+//              and its MMAs stream back to back.
+//   warp 8     TMEM allocation (2 x N columns) and the single MMA-issuing thread; tile i
 //              accumulates into TMEM buffer i % 2.
-//   warps 5-8  epilogue: tcgen05.ld of the finished buffer -> scale -> BF16 -> a shared-memory
+//   warps 9-12 epilogue: tcgen05.ld of the finished buffer -> scale -> BF16 -> a shared-memory
 //              copy of the output tile -> one bulk async store of the tile's contiguous rows;
 //              overlaps the next tile's main loop.
-//   warp 9     loader: bulk async copies of each tile's map rows (double-buffered) and of each
+//   warp 13    loader: bulk async copies of each tile's map rows (double-buffered) and of each
 //              step's pre-packed, pre-swizzled weight tiles.
 //
 // Every mbarrier wait is bounded (about a second); on expiry the CTA stops, waits for its
@@ -45,7 +48,11 @@ using namespace tc;
 constexpr int kTileM = 128;
 constexpr int kRowBytes = 128;  // one swizzle row = 64 bf16 or 128 fp8 elements
 constexpr int kABytes = kTileM * kRowBytes;
-constexpr int kThreads = 320;  // 4 gather + 1 MMA + 4 epilogue + 1 loader warps
+constexpr int kGatherWarps = 8;   // 256 gather threads: cp.async throughput grows with the issuing warps
+constexpr int kRowsPerWarp = kTileM / kGatherWarps;
+constexpr int kMmaWarp = kGatherWarps;
+constexpr int kEpiWarps = 4;
+constexpr int kThreads = (kGatherWarps + 1 + kEpiWarps + 1) * 32;  // + loader warp
 constexpr int kMaxMapStage = 32;  // map tiles staged in shared memory up to K = 32
 constexpr int kLag = 2;  // cp.async groups a gather thread keeps in flight before publishing a stage
 
@@ -112,11 +119,12 @@ struct StepWalker {
         }
         return k_lin < a.K ? k_lin++ : -1;
     }
-    // fills ks[0..pack) (-1 for absent) and the chunk index
+    // fills ks[0..PACK) (-1 for absent) and the chunk index
+    template <int PACK>
     __device__ __forceinline__ void next(const FwdArgs &a, int (&ks)[4], int &c) {
-        if (a.pack > 1) {
+        if (PACK > 1) {
 #pragma unroll
-            for (int p = 0; p < 4; ++p) ks[p] = p < a.pack ? pop(a) : -1;
+            for (int p = 0; p < 4; ++p) ks[p] = p < PACK ? pop(a) : -1;
             c = 0;
             return;
         }
@@ -128,13 +136,23 @@ struct StepWalker {
     }
 };
 
-template <int BN, int EBYTES>
+__device__ __forceinline__ void st_shared_zero16(uint32_t addr) {
+    asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(addr), "r"(0) : "memory");
+}
+
+__device__ __forceinline__ int pick(const int (&ks)[4], int p) {
+    return p == 0 ? ks[0] : (p == 1 ? ks[1] : (p == 2 ? ks[2] : ks[3]));
+}
+
+template <int BN, int EBYTES, int PACK>
 __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr int kBTile = BN * kRowBytes;
+    constexpr int kStage = kABytes + PACK * kBTile;
+    constexpr int kSlotBytes = kRowBytes / PACK;            // one offset's share of an A row (PACK > 1)
+    constexpr int kCpr = PACK > 1 ? kSlotBytes / 16 : 8;    // 16-byte chunks per offset slot
     const int S = a.stages;
-    const int kStage = kABytes + a.pack * kBTile;
     const bool stage_map = a.K <= kMaxMapStage;
     const int map_words = stage_map ? kTileM * a.K : 0;  // per buffer; 512*K bytes, 16-byte aligned
     int32_t *map_sm = reinterpret_cast<int32_t *>(smem + S * kStage);
@@ -151,87 +169,127 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full[s], kTileM + 1);  // 128 gather threads + the loader's expect_tx
+            mbar_init(&full[s], kGatherWarps + 1);  // one lane per gather warp + the loader's expect_tx
             mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], kTileM);
+            mbar_init(&tempty[b], kEpiWarps);  // one lane per epilogue warp
             mbar_init(&mfull[b], 1);
-            mbar_init(&mempty[b], kTileM);
+            mbar_init(&mempty[b], kGatherWarps);
         }
         mbar_init(fin, 1);
         *abort = 0;
     }
-    if (warp == 4) tmem_alloc(tmem_slot, kTmemCols);
+    if (warp == kMmaWarp) tmem_alloc(tmem_slot, kTmemCols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp < 4) {
+    if (warp < kGatherWarps) {
         // ----------------------------------------------------------------- gather (A operand)
-        const int r = threadIdx.x;
+        // Lane -> (16-byte chunk j of the 128-byte A row, rows rsub, rsub+4, rsub+8, rsub+12 of
+        // this warp's 16): one warp instruction moves four whole A rows.
         const uint64_t keep = policy_evict_last();
-        uint32_t it = 0, sig = 0;
+        const int j = lane & 7;
+        const int rsub = lane >> 3;
+        const int row0 = warp * kRowsPerWarp;
+        const int slot = j / kCpr;         // offset slot of chunk j
+        const int jj = j - slot * kCpr;    // chunk within that offset's row
+        uint32_t it = 0, sig = 0, stage = 0, phase = 0, pstage = 0;
         int64_t tile = blockIdx.x;
         uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
         for (int i = 0; tile < a.n_tiles && !*abort; tile += stride, ++i) {
             const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
-            const int64_t row = tile * kTileM + r;
             const int mb = i & 1;
-            if (stage_map && !mbar_wait(&mfull[mb], (i >> 1) & 1, abort)) break;
-            const int32_t *mrow = map_sm + mb * map_words + r * a.K;
+            if (stage_map && !__all_sync(0xffffffffu, mbar_wait_backoff(&mfull[mb], (i >> 1) & 1, abort, 64))) break;
+            const int32_t *mtile = map_sm + mb * map_words;
             const Steps st = make_steps(a, mask_cur);
             StepWalker w{st.kbits, 0, 0, -1};
             bool ok = true;
             for (int s = 0; s < st.n_steps; ++s) {
                 int ks[4], c;
-                w.next(a, ks, c);
-                const int stage = it % S;
-                if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) {
+                w.template next<PACK>(a, ks, c);
+                const int k = PACK == 1 ? ks[0] : pick(ks, slot);
+                const int bytes = PACK > 1 ? kSlotBytes : min(kRowBytes, a.row_bytes - c * kRowBytes);
+                // unused offset slots and bytes past a short last chunk are never read by the MMA
+                const bool on = k >= 0 && (PACK > 1 || j * 16 < bytes);
+                const int64_t colb = PACK > 1 ? (int64_t)jj * 16 : (int64_t)c * kRowBytes + j * 16;
+                // map entries first: their latency overlaps the wait for the stage
+                int32_t src[kRowsPerWarp / 4];
+#pragma unroll
+                for (int q = 0; q < kRowsPerWarp / 4; ++q) {
+                    const int r = row0 + rsub + 4 * q;
+                    int32_t v = -1;
+                    if (on) {
+                        if (stage_map) {
+                            v = mtile[r * a.K + k];
+                        } else {
+                            const int64_t row = tile * kTileM + r;
+                            v = row < a.n_out ? a.map[row * a.K + k] : -1;
+                        }
+                    }
+                    src[q] = v;
+                }
+                bool go = true;
+                if (lane == 0) go = mbar_wait(&empty[stage], phase ^ 1, abort);
+                go = __shfl_sync(0xffffffffu, go, 0);
+                __syncwarp();
+                if (!go) {
                     ok = false;
                     break;
                 }
                 const uint32_t As = smem_u32(smem + stage * kStage);
 #pragma unroll
-                for (int p = 0; p < 4; ++p) {
-                    if (p >= a.pack || ks[p] < 0) continue;
-                    int32_t src;
-                    if (stage_map) {
-                        src = mrow[ks[p]];
-                    } else {
-                        src = row < a.n_out ? a.map[row * a.K + ks[p]] : -1;
-                    }
-                    if (src >= a.n_x) src = -1;
-                    const uint8_t *g = a.x + (src >= 0 ? (int64_t)src * a.ldx_bytes + (int64_t)c * kRowBytes : 0);
-                    const int bytes = min(kRowBytes, a.row_bytes - c * kRowBytes);
-                    const int j0 = p * (a.row_bytes >> 4);
-                    for (int j = 0; j < (bytes >> 4); ++j)
-                        cp_async_16_hint(As + sw128_offset(r, j0 + j), g + j * 16, src >= 0 ? 16u : 0u, keep);
+                for (int q = 0; q < kRowsPerWarp / 4; ++q) {
+                    if (!on) continue;
+                    const uint32_t dst = As + sw128_offset(row0 + rsub + 4 * q, j);
+                    if (src[q] >= 0 && src[q] < a.n_x)
+                        cp_async_16_hint(dst, a.x + (int64_t)src[q] * a.ldx_bytes + colb, 16u, keep);
+                    else
+                        st_shared_zero16(dst);
                 }
                 cp_async_commit();
                 ++it;
+                if (++stage == (uint32_t)S) {
+                    stage = 0;
+                    phase ^= 1;
+                }
                 if (it - sig > kLag) {
                     // the copies of step `sig` have landed: publish them to the async proxy (tcgen05.mma)
                     cp_async_wait_group<kLag>();
                     fence_proxy_async();
-                    mbar_arrive(&full[sig % S]);
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&full[pstage]);
                     ++sig;
+                    if (++pstage == (uint32_t)S) pstage = 0;
                 }
             }
-            if (stage_map) mbar_arrive(&mempty[mb]);
+            __syncwarp();
+            if (stage_map && lane == 0) mbar_arrive(&mempty[mb]);
             if (!ok) break;
             mask_cur = mask_next;
         }
         cp_async_wait_group<0>();
         fence_proxy_async();
-        for (; sig < it; ++sig) mbar_arrive(&full[sig % S]);
-    } else if (warp == 4) {
+        __syncwarp();
+        if (lane == 0)
+            for (; sig < it; ++sig) {
+                mbar_arrive(&full[pstage]);
+                if (++pstage == (uint32_t)S) pstage = 0;
+            }
+    } else if (warp == kMmaWarp) {
         // ----------------------------------------------------------------- MMA issuer
+        // Descriptors are advanced by constant offsets (16-byte units) from one base: shared
+        // addresses stay below 2^18, so the 14-bit start-address field never carries.
         if (lane == 0) {
             constexpr uint32_t idesc = EBYTES == 2 ? idesc_m128(BN, 1, 1) : idesc_m128(BN, 0, 0);
-            uint32_t it = 0;
+            constexpr uint32_t kStageD = kStage >> 4, kBOffD = kABytes >> 4, kBTileD = kBTile >> 4,
+                               kSlotD = kSlotBytes >> 4;
+            const uint64_t adesc0 = desc_sw128(smem_u32(smem));
+            const int last_k32 = (a.row_bytes - (a.nchunks - 1) * kRowBytes) >> 5;  // PACK == 1: last chunk
+            uint32_t stage = 0, phase = 0;
             bool ok = true;
             int64_t tile = blockIdx.x;
             uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
@@ -242,35 +300,47 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                 tc_fence_after();
                 const uint32_t d = tmem + b * BN;
                 const Steps st = make_steps(a, mask_cur);
-                StepWalker w{st.kbits, 0, 0, -1};
                 uint32_t acc = 0;
-                for (int s = 0; s < st.n_steps; ++s, ++it) {
-                    int ks[4], c;
-                    w.next(a, ks, c);
-                    const int stage = it % S;
-                    if (!mbar_wait(&full[stage], (it / S) & 1, abort)) {
+                int c = 0;
+                for (int s = 0; s < st.n_steps; ++s) {
+                    if (!mbar_wait(&full[stage], phase, abort)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t As = smem_u32(smem + stage * kStage);
-                    const int bytes = min(kRowBytes, a.row_bytes - c * kRowBytes);
-                    int q = 0;
+                    const uint64_t ad = adesc0 + stage * kStageD, bd = ad + kBOffD;
+                    if (PACK > 1) {
+                        const int slots = min(PACK, st.n_act - s * PACK);
 #pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        if (p >= a.pack || ks[p] < 0) continue;
-                        const uint32_t Ap = As + p * a.row_bytes, Bp = As + kABytes + q * kBTile;
-                        for (int h = 0; h < (bytes >> 5); ++h) {  // 32 bytes of K per MMA
-                            const uint64_t ad = desc_sw128(Ap + h * 32), bd = desc_sw128(Bp + h * 32);
+                        for (int p = 0; p < PACK; ++p) {
+                            if (p >= slots) break;
+#pragma unroll
+                            for (int h = 0; h < kSlotBytes / 32; ++h) {  // 32 bytes of K per MMA
+                                if (EBYTES == 2)
+                                    mma_f16(d, ad + p * kSlotD + 2 * h, bd + p * kBTileD + 2 * h, idesc, acc);
+                                else
+                                    mma_f8(d, ad + p * kSlotD + 2 * h, bd + p * kBTileD + 2 * h, idesc, acc);
+                                acc = 1;
+                            }
+                        }
+                    } else {
+                        const int nk = c == a.nchunks - 1 ? last_k32 : 4;
+#pragma unroll
+                        for (int h = 0; h < 4; ++h) {
+                            if (h >= nk) break;
                             if (EBYTES == 2)
-                                mma_f16(d, ad, bd, idesc, acc);
+                                mma_f16(d, ad + 2 * h, bd + 2 * h, idesc, acc);
                             else
-                                mma_f8(d, ad, bd, idesc, acc);
+                                mma_f8(d, ad + 2 * h, bd + 2 * h, idesc, acc);
                             acc = 1;
                         }
-                        ++q;
+                        c = c + 1 == a.nchunks ? 0 : c + 1;
                     }
                     mma_commit(&empty[stage]);
+                    if (++stage == (uint32_t)S) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
                 }
                 if (!ok) break;
                 if (acc)
@@ -282,21 +352,22 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
             // all issued MMAs complete before TMEM is released
             mma_commit(fin);
             const long long t0 = clock64();
-            while (!mbar_try_wait(fin, 0) && clock64() - t0 < kWaitCycles) {
+            while (!mbar_try_wait_sleep(fin, 0, kSuspendNs) && clock64() - t0 < kWaitCycles) {
             }
         }
         __syncwarp();
-    } else if (warp < 9) {
+    } else if (warp < kMmaWarp + 1 + kEpiWarps) {
         // ----------------------------------------------------------------- epilogue
-        const int et = threadIdx.x - 160;  // 0..127
-        const int q4 = warp & 3;           // TMEM lane quarter this warp may access
-        const int rt = q4 * 32 + lane;     // row of the tile this thread drains
+        const int et = threadIdx.x - (kMmaWarp + 1) * 32;  // 0..127
+        const int q4 = warp & 3;                           // TMEM lane quarter this warp may access
+        const int rt = q4 * 32 + lane;                     // row of the tile this thread drains
         int64_t tile = blockIdx.x;
         uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
         for (int i = 0; tile < a.n_tiles; tile += stride, ++i) {
             const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
             const int b = i & 1;
-            const bool ready = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (i >> 1) & 1, abort) && !*abort);
+            const bool ready =
+                __all_sync(0xffffffffu, mbar_wait_backoff(&tfull[b], (i >> 1) & 1, abort, 128) && !*abort);
             if (!ready) break;
             tc_fence_after();
             const Steps st = make_steps(a, mask_cur);
@@ -337,12 +408,17 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                     if (c0 + 8 < a.cout) dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                 } else {
                     __nv_bfloat16 *yrow = reinterpret_cast<__nv_bfloat16 *>(a.y) + (m0 + rt) * a.ldy;
-                    const __nv_bfloat16 *hv = reinterpret_cast<const __nv_bfloat16 *>(packed);
-                    for (int t = 0; t < 16 && c0 + t < a.cout; ++t) yrow[c0 + t] = hv[t];
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) {
+                        const __nv_bfloat162 h2 = *reinterpret_cast<const __nv_bfloat162 *>(&packed[t]);
+                        if (c0 + 2 * t < a.cout) yrow[c0 + 2 * t] = h2.x;
+                        if (c0 + 2 * t + 1 < a.cout) yrow[c0 + 2 * t + 1] = h2.y;
+                    }
                 }
             }
             tc_fence_before();
-            mbar_arrive(&tempty[b]);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[b]);
             if (a.direct_store) {
                 fence_proxy_async();  // staging writes -> visible to the bulk store (async proxy)
                 named_barrier(1, kTileM);
@@ -357,7 +433,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
     } else {
         // ----------------------------------------------------------------- loader (bulk copies)
         if (lane == 0) {
-            uint32_t it = 0;
+            uint32_t stage = 0, phase = 0;
             int64_t tile = blockIdx.x;
             const uint32_t map_bytes = (uint32_t)map_words * 4;
             if (stage_map && tile < a.n_tiles) {
@@ -370,33 +446,34 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                 const uint32_t mask_next = nxt < a.n_tiles ? load_mask(a, nxt) : 0;
                 if (stage_map && nxt < a.n_tiles) {
                     const int nb = (i + 1) & 1;
-                    if (!mbar_wait(&mempty[nb], (((i + 1) >> 1) & 1) ^ 1, abort)) break;
+                    if (!mbar_wait_backoff(&mempty[nb], (((i + 1) >> 1) & 1) ^ 1, abort, 32)) break;
                     mbar_arrive_expect_tx(&mfull[nb], map_bytes);
                     bulk_g2s(smem_u32(map_sm + nb * map_words), a.map + nxt * kTileM * a.K, map_bytes, &mfull[nb]);
                 }
                 const Steps st = make_steps(a, mask_cur);
                 StepWalker w{st.kbits, 0, 0, -1};
                 bool ok = true;
-                for (int s = 0; s < st.n_steps; ++s, ++it) {
+                for (int s = 0; s < st.n_steps; ++s) {
                     int ks[4], c;
-                    w.next(a, ks, c);
-                    const int stage = it % S;
-                    if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) {
+                    w.template next<PACK>(a, ks, c);
+                    if (!mbar_wait(&empty[stage], phase ^ 1, abort)) {
                         ok = false;
                         break;
                     }
                     int nb = 0;
 #pragma unroll
-                    for (int p = 0; p < 4; ++p) nb += (p < a.pack && ks[p] >= 0) ? 1 : 0;
+                    for (int p = 0; p < PACK; ++p) nb += ks[p] >= 0 ? 1 : 0;
                     mbar_arrive_expect_tx(&full[stage], nb * kBTile);
                     const uint32_t Bs = smem_u32(smem + stage * kStage) + kABytes;
-                    int q = 0;
 #pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        if (p >= a.pack || ks[p] < 0) continue;
-                        bulk_g2s(Bs + q * kBTile, a.wpack + ((int64_t)ks[p] * a.nchunks + c) * kBTile, kBTile,
+                    for (int p = 0; p < PACK; ++p) {
+                        if (ks[p] < 0) break;
+                        bulk_g2s(Bs + p * kBTile, a.wpack + ((int64_t)ks[p] * a.nchunks + c) * kBTile, kBTile,
                                  &full[stage]);
-                        ++q;
+                    }
+                    if (++stage == (uint32_t)S) {
+                        stage = 0;
+                        phase ^= 1;
                     }
                 }
                 if (!ok) break;
@@ -407,7 +484,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4) {
+    if (warp == kMmaWarp) {
         tc_fence_after();
         tmem_dealloc(tmem, kTmemCols);
     }
@@ -464,9 +541,9 @@ int sm_count() {
     return cache[dev];
 }
 
-template <int BN, int EB>
+template <int BN, int EB, int PACK>
 int launch_fwd(FwdArgs a, cudaStream_t s) {
-    const int stage = kABytes + a.pack * BN * kRowBytes;
+    const int stage = kABytes + PACK * BN * kRowBytes;
     const int map_bytes = a.K <= kMaxMapStage ? 2 * kTileM * a.K * 4 : 0;
     a.direct_store = (a.direct_store && BN <= 128) ? 1 : 0;  // staging tile only where it fits
     const int fixed = 1024 + map_bytes + (a.direct_store ? kTileM * BN * 2 : 0) + (2 * 8 + 9) * 8 + 16;
@@ -476,13 +553,36 @@ int launch_fwd(FwdArgs a, cudaStream_t s) {
     if (stages < kLag + 1 || stages * stage + fixed > 227 * 1024) return FVGB_EINVAL;
     a.stages = stages;
     const int smem = stages * stage + fixed;
-    auto kern = conv_tc_fwd_kernel<BN, EB>;
+    auto kern = conv_tc_fwd_kernel<BN, EB, PACK>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
         return launch_status();
     const int64_t grid = std::min<int64_t>(a.n_tiles, sm_count());
     kern<<<(unsigned)grid, kThreads, smem, s>>>(a);
     count_launches(1);
     return launch_status();
+}
+
+template <int EB, int PACK>
+int dispatch_bn(int BN, FwdArgs a, cudaStream_t s) {
+    switch (BN) {
+        case 32: return launch_fwd<32, EB, PACK>(a, s);
+        case 64: return launch_fwd<64, EB, PACK>(a, s);
+        case 128: return launch_fwd<128, EB, PACK>(a, s);
+        default: return launch_fwd<256, EB, PACK>(a, s);
+    }
+}
+
+template <int EB>
+int dispatch_pack(int BN, int pack, FwdArgs a, cudaStream_t s) {
+    switch (pack) {
+        case 1: return dispatch_bn<EB, 1>(BN, a, s);
+        case 2: return dispatch_bn<EB, 2>(BN, a, s);
+        default: return dispatch_bn<EB, 4>(BN, a, s);
+    }
+}
+
+int dispatch_fwd(int eb, int BN, int pack, FwdArgs a, cudaStream_t s) {
+    return eb == 2 ? dispatch_pack<2>(BN, pack, a, s) : dispatch_pack<1>(BN, pack, a, s);
 }
 
 }  // namespace
@@ -560,18 +660,5 @@ extern "C" int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32
     a.n_tiles = ceil_div(n_out, kTileM);
     a.direct_store = (ldy == c_out && c_out % 8 == 0) ? 1 : 0;
     cudaStream_t s = as_stream(stream);
-    if (eb == 2) {
-        switch (BN) {
-            case 32: return launch_fwd<32, 2>(a, s);
-            case 64: return launch_fwd<64, 2>(a, s);
-            case 128: return launch_fwd<128, 2>(a, s);
-            default: return launch_fwd<256, 2>(a, s);
-        }
-    }
-    switch (BN) {
-        case 32: return launch_fwd<32, 1>(a, s);
-        case 64: return launch_fwd<64, 1>(a, s);
-        case 128: return launch_fwd<128, 1>(a, s);
-        default: return launch_fwd<256, 1>(a, s);
-    }
+    return dispatch_fwd(eb, BN, a.pack, a, s);
 }

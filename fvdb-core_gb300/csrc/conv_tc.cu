@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full[s], kTileM);  // one arrival per gather thread
+            mbar_init(&full[s], kTileM / 32);  // one arrival per gather warp
             mbar_init(&empty[s], 1);
         }
         mbar_init(accum, 1);
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
         for (int64_t t = 0; t < n_tiles && !*abort; ++t) {
             if (!tile_active(t)) continue;
             const int stage = it % S;
-            if (!mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort)) break;
+            if (!__all_sync(0xffffffffu, mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort))) break;
             const uint32_t base = smem_u32(smem + stage * kStage);
             const int64_t m = r_begin + t * kTileM + r;
             const bool row_ok = m < r_end;
@@ -188,20 +188,24 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
                 for (int e = 0; e < a.cin; e += 8)
                     cp_async_16(base + mn_offset(r, j * a.cin + e), xrow + e * 2, src >= 0 ? 16u : 0u);
             }
-            // cp.async writes are generic-proxy writes: each thread publishes a stage to the
-            // tensor core (async proxy) itself, one step late, so the MMA thread never fences
+            // cp.async writes are generic-proxy writes: each thread fences its own copies to the
+            // tensor core (async proxy), one step late, so the MMA thread never fences; one lane
+            // per warp then arrives (per-thread arrivals on one barrier word serialise)
             cp_async_commit();
             ++it;
             if (it - sig > 1) {
                 cp_async_wait_group<1>();
                 fence_proxy_async();
-                mbar_arrive(&full[sig % S]);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[sig % S]);
                 ++sig;
             }
         }
         cp_async_wait_group<0>();
         fence_proxy_async();
-        for (; sig < it; ++sig) mbar_arrive(&full[sig % S]);
+        __syncwarp();
+        if (lane == 0)
+            for (; sig < it; ++sig) mbar_arrive(&full[sig % S]);
     } else if (warp == 4 && lane == 0) {
         constexpr uint32_t idesc = idesc_m128(BN, 1, 1) | (1u << 15) | (1u << 16);  // bf16, A and B MN-major
         int it = 0;

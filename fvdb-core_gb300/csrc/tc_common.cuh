@@ -28,8 +28,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
+// try_wait that lets the hardware suspend the thread until the phase completes or `ns`
+// nanoseconds pass.  Without the hint a waiting thread re-polls almost at once, and many
+// polling threads (e.g. epilogue warps idle for a whole tile) flood the shared-memory pipe
+// that the gather copies and tcgen05 instructions of the busy warps also go through.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity, uint32_t ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+
 // Spin budget of every wait: ~2^31 SM cycles (about one second at GB300 clocks).
 constexpr long long kWaitCycles = 1ll << 31;
+// Longest hardware suspension of one try_wait (ns); the abort flag and the budget are
+// checked between suspensions.
+constexpr uint32_t kSuspendNs = 1000000;
 
 // Waits for the phase of `parity` to complete.  Returns false (and raises *abort) if it did
 // not within kWaitCycles or if another thread of the CTA already aborted.
@@ -37,6 +56,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
+        if (mbar_try_wait_sleep(bar, parity, kSuspendNs)) return true;
+        if (*abort) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abort = 1;
+            return false;
+        }
+    }
+}
+
+// mbar_wait for waits off the critical path (a warp idle for a whole tile): between polls the
+// warp sleeps `ns` nanoseconds, leaving the issue slots of its SM sub-partition to busy warps.
+__device__ __forceinline__ bool mbar_wait_backoff(uint64_t *bar, uint32_t parity, volatile int *abort, uint32_t ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (true) {
+        __nanosleep(ns);
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort) return false;
         if (clock64() - t0 > kWaitCycles) {

@@ -124,7 +124,7 @@ def test_finite_differences_fp64_and_bf16_gradients(cuda_device):
     #     of the ~0.2 % of pre-activations within rounding distance of zero, and each flip drops or
     #     adds a whole gradient term: ~4 % rel-L2 on dx and dW1 (the same 3.9 % comes out of a CPU
     #     emulation of BF16 storage with the FP64 oracle), so the bound here is 6e-2.
-    assert rel_l2(y16.double().cpu().numpy(), net(fvdb.nn.VDBTensor(grid, grid.jagged_like(x))).data.jdata.detach().cpu().numpy()) <= 1e-2
+    assert rel_l2(y16.detach().double().cpu().numpy(), net(fvdb.nn.VDBTensor(grid, grid.jagged_like(x))).data.jdata.detach().cpu().numpy()) <= 1e-2
     assert rel_l2(x16.grad.double().cpu().numpy(), gx.cpu().numpy()) <= 6e-2
     assert rel_l2(d1.weight.grad.double().cpu().numpy(), gw1.cpu().numpy()) <= 6e-2
     # (b) against FP64 arithmetic on the same BF16-rounded operands and activations (same masks):
