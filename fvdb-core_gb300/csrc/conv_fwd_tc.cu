@@ -4,10 +4,13 @@
 //
 // Persistent kernel, one CTA per SM, looping over 128-row output tiles (tile t = blockIdx.x +
 // i * gridDim.x).  Each tile owns all (<= 256) output channels, so every output row is written
-// exactly once, without atomics.  The reduction dimension runs over (kernel offset, 128-byte
-// channel chunk); when a feature row is shorter than 128 bytes (c_in*elem = 64 or 32 bytes),
-// two or four kernel offsets share one 128-byte swizzle row of the A operand.  Offsets absent
-// from all 128 rows of a tile (per-tile occupancy mask) are skipped.
+// exactly once, without atomics.  The reduction dimension is cut into units of 128 bytes: one
+// 128-byte channel chunk of one kernel offset, or, when a feature row is 64 or 32 bytes, a fixed
+// group of 2 or 4 consecutive offsets whose rows share one 128-byte A row (one weight image per
+// group, so no half-empty weight tiles).  Units absent from all 128 rows of a tile (per-tile
+// occupancy mask) are skipped.  A pipeline stage carries U units (2 for N <= 64), so every
+// barrier round trip feeds 8 MMAs: the per-stage handshakes, not bytes, set the pace of this
+// kernel, and tcgen05.mma with N <= 128 costs the same ~60-80 cycles whatever N is.
 //
 // Warp roles (448 threads):
 //   warps 0-7  gather: each warp fills 16 rows of the A tile.  Lane l copies 16-byte chunk l%8 of
@@ -19,14 +22,15 @@
 //              with st.shared.  Both are generic-proxy writes, so each warp publishes a stage to
 //              the tensor core (async proxy) itself, kLag steps late: cp.async.wait_group,
 //              fence.proxy.async, __syncwarp, one mbarrier arrive.  The MMA thread never fences
-//              and its MMAs stream back to back.
+//              and its MMAs stream back to back.  Map entries are read before the stage wait so
+//              their latency overlaps it.
 //   warp 8     TMEM allocation (2 x N columns) and the single MMA-issuing thread; tile i
 //              accumulates into TMEM buffer i % 2.
 //   warps 9-12 epilogue: tcgen05.ld of the finished buffer -> scale -> BF16 -> a shared-memory
 //              copy of the output tile -> one bulk async store of the tile's contiguous rows;
 //              overlaps the next tile's main loop.
 //   warp 13    loader: bulk async copies of each tile's map rows (double-buffered) and of each
-//              step's pre-packed, pre-swizzled weight tiles.
+//              unit's pre-packed, pre-swizzled weight image.
 //
 // Every mbarrier wait is bounded (about a second); on expiry the CTA stops, waits for its
 // issued work, frees TMEM and raises *err = FVGB_ETIMEOUT.
@@ -54,8 +58,12 @@ constexpr int kMmaWarp = kGatherWarps;
 constexpr int kEpiWarps = 4;
 constexpr int kThreads = (kGatherWarps + 1 + kEpiWarps + 1) * 32;  // + loader warp
 constexpr int kMaxMapStage = 32;  // map tiles staged in shared memory up to K = 32
-constexpr int kLag = 2;  // cp.async groups a gather thread keeps in flight before publishing a stage
+constexpr int kLag = 1;  // cp.async groups a gather thread keeps in flight before publishing a stage
 
+// A "unit" is 128 bytes of the reduction dimension for all 128 rows of a tile: one 128-byte
+// channel chunk of one kernel offset (rows of >= 128 bytes), or a fixed group of `pack`
+// consecutive offsets whose rows share one 128-byte A row (rows of 64 or 32 bytes).  Each unit
+// has one pre-packed [BN x 128 B] weight image; a pipeline stage holds U units.
 struct FwdArgs {
     const uint8_t *x;
     int64_t n_x;
@@ -65,72 +73,81 @@ struct FwdArgs {
     int64_t n_out;
     int32_t K;
     const uint32_t *tile_mask;  // may be null (or K > 32): no skipping
-    const uint8_t *wpack;       // [K][nchunks][BN rows][128 B]
-    int32_t nchunks;
-    int32_t pack;        // kernel offsets per 128-byte A row (1, 2 or 4); pack > 1 => nchunks == 1
-    int32_t row_bytes;   // c_in * elem
+    const uint8_t *wpack;       // [units][BN rows][128 B]
+    int32_t nchunks;            // 128-byte chunks per row (pack == 1)
+    int32_t pack;               // kernel offsets per 128-byte A row (1, 2 or 4); pack > 1 => nchunks == 1
+    int32_t groups;             // offset groups (pack > 1): ceil(K / pack)
+    int32_t row_bytes;          // c_in * elem
     int32_t cout;
-    uint8_t *y;          // bf16 [n_out, ldy]
+    uint8_t *y;                 // bf16 [n_out, ldy]
     int64_t ldy;
-    const float *scale;  // per output channel, may be null
+    const float *scale;         // per output channel, may be null
     int32_t *err;
     int32_t stages;
     int64_t n_tiles;
     int32_t direct_store;  // 1: output rows contiguous (ldy == cout, cout % 8 == 0): one bulk store per tile
 };
 
-struct Steps {
-    uint32_t kbits;  // active offsets (K <= 32)
-    int n_act;       // number of active offsets
-    int n_steps;
+// Active units of one tile: a bit set (K <= 32 with a mask) or all units in order.
+struct Units {
+    uint32_t bits;  // pack > 1: active groups; pack == 1: active offsets
+    int n;          // number of units
 };
 
-__device__ __forceinline__ uint32_t load_mask(const FwdArgs &a, int64_t tile) {
-    if (a.K > 32) return 0;
+template <int PACK>
+__device__ __forceinline__ Units tile_units(const FwdArgs &a, int64_t tile) {
+    Units u;
+    if (a.K > 32) {
+        u.bits = 0;
+        u.n = PACK > 1 ? a.groups : a.K * a.nchunks;
+        return u;
+    }
     const uint32_t all = a.K == 32 ? 0xffffffffu : ((1u << a.K) - 1u);
-    return a.tile_mask ? (__ldg(a.tile_mask + tile) & all) : all;
-}
-
-__device__ __forceinline__ Steps make_steps(const FwdArgs &a, uint32_t mask) {
-    Steps s;
-    if (a.K <= 32) {
-        s.kbits = mask;
-        s.n_act = __popc(mask);
+    const uint32_t mask = a.tile_mask ? (__ldg(a.tile_mask + tile) & all) : all;
+    if (PACK > 1) {
+        uint32_t gm = 0;
+        for (int g = 0; g < a.groups; ++g)
+            if ((mask >> (g * PACK)) & ((1u << PACK) - 1u)) gm |= 1u << g;
+        u.bits = gm;
+        u.n = __popc(gm);
     } else {
-        s.kbits = 0;
-        s.n_act = a.K;
+        u.bits = mask;
+        u.n = __popc(mask) * a.nchunks;
     }
-    s.n_steps = a.pack > 1 ? (s.n_act + a.pack - 1) / a.pack : s.n_act * a.nchunks;
-    return s;
+    return u;
 }
 
-// Walks the (offset, chunk) sequence of a tile; next() returns the offsets of one step.
-struct StepWalker {
-    uint32_t kb;
-    int k_lin;  // offset counter when K > 32
-    int chunk;
-    int cur_k;
-    __device__ __forceinline__ int pop(const FwdArgs &a) {
-        if (a.K <= 32) {
-            if (!kb) return -1;
-            const int k = __ffs(kb) - 1;
-            kb &= kb - 1;
-            return k;
-        }
-        return k_lin < a.K ? k_lin++ : -1;
-    }
-    // fills ks[0..PACK) (-1 for absent) and the chunk index
-    template <int PACK>
-    __device__ __forceinline__ void next(const FwdArgs &a, int (&ks)[4], int &c) {
+// Walks a tile's units in order: the weight image index, the first kernel offset and the chunk.
+template <int PACK>
+struct UnitWalker {
+    uint32_t bits;
+    int lin;    // unit counter when K > 32
+    int chunk;  // pack == 1
+    int cur;    // pack == 1: current offset
+    __device__ __forceinline__ void next(const FwdArgs &a, int &image, int &k0, int &c) {
         if (PACK > 1) {
-#pragma unroll
-            for (int p = 0; p < 4; ++p) ks[p] = p < PACK ? pop(a) : -1;
+            int g;
+            if (a.K <= 32) {
+                g = __ffs(bits) - 1;
+                bits &= bits - 1;
+            } else {
+                g = lin++;
+            }
+            image = g;
+            k0 = g * PACK;
             c = 0;
             return;
         }
-        if (chunk == 0) cur_k = pop(a);
-        ks[0] = cur_k;
-        ks[1] = ks[2] = ks[3] = -1;
+        if (chunk == 0) {
+            if (a.K <= 32) {
+                cur = __ffs(bits) - 1;
+                bits &= bits - 1;
+            } else {
+                cur = lin++;
+            }
+        }
+        image = cur * a.nchunks + chunk;
+        k0 = cur;
         c = chunk;
         chunk = (chunk + 1 == a.nchunks) ? 0 : chunk + 1;
     }
@@ -140,18 +157,15 @@ __device__ __forceinline__ void st_shared_zero16(uint32_t addr) {
     asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(addr), "r"(0) : "memory");
 }
 
-__device__ __forceinline__ int pick(const int (&ks)[4], int p) {
-    return p == 0 ? ks[0] : (p == 1 ? ks[1] : (p == 2 ? ks[2] : ks[3]));
-}
-
-template <int BN, int EBYTES, int PACK>
+template <int BN, int EBYTES, int PACK, int U>
 __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr int kBTile = BN * kRowBytes;
-    constexpr int kStage = kABytes + PACK * kBTile;
-    constexpr int kSlotBytes = kRowBytes / PACK;            // one offset's share of an A row (PACK > 1)
-    constexpr int kCpr = PACK > 1 ? kSlotBytes / 16 : 8;    // 16-byte chunks per offset slot
+    constexpr int kStage = U * (kABytes + kBTile);          // [U A tiles][U B tiles]
+    constexpr int kSlotBytes = kRowBytes / PACK;             // one offset's share of an A row
+    constexpr int kCpr = PACK > 1 ? kSlotBytes / 16 : 8;     // 16-byte chunks per offset slot
+    constexpr int kCopies = kRowsPerWarp / 4;                // rows per lane per unit
     const int S = a.stages;
     const bool stage_map = a.K <= kMaxMapStage;
     const int map_words = stage_map ? kTileM * a.K : 0;  // per buffer; 512*K bytes, 16-byte aligned
@@ -195,42 +209,46 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
         const int j = lane & 7;
         const int rsub = lane >> 3;
         const int row0 = warp * kRowsPerWarp;
-        const int slot = j / kCpr;         // offset slot of chunk j
+        const int slot = j / kCpr;         // offset slot of chunk j within a group
         const int jj = j - slot * kCpr;    // chunk within that offset's row
         uint32_t it = 0, sig = 0, stage = 0, phase = 0, pstage = 0;
         int64_t tile = blockIdx.x;
-        uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
         for (int i = 0; tile < a.n_tiles && !*abort; tile += stride, ++i) {
-            const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
             const int mb = i & 1;
             if (stage_map && !__all_sync(0xffffffffu, mbar_wait_backoff(&mfull[mb], (i >> 1) & 1, abort, 64))) break;
             const int32_t *mtile = map_sm + mb * map_words;
-            const Steps st = make_steps(a, mask_cur);
-            StepWalker w{st.kbits, 0, 0, -1};
+            const Units un = tile_units<PACK>(a, tile);
+            UnitWalker<PACK> w{un.bits, 0, 0, -1};
             bool ok = true;
-            for (int s = 0; s < st.n_steps; ++s) {
-                int ks[4], c;
-                w.template next<PACK>(a, ks, c);
-                const int k = PACK == 1 ? ks[0] : pick(ks, slot);
-                const int bytes = PACK > 1 ? kSlotBytes : min(kRowBytes, a.row_bytes - c * kRowBytes);
-                // unused offset slots and bytes past a short last chunk are never read by the MMA
-                const bool on = k >= 0 && (PACK > 1 || j * 16 < bytes);
-                const int64_t colb = PACK > 1 ? (int64_t)jj * 16 : (int64_t)c * kRowBytes + j * 16;
+            for (int u0 = 0; u0 < un.n; u0 += U) {
                 // map entries first: their latency overlaps the wait for the stage
-                int32_t src[kRowsPerWarp / 4];
+                int32_t src[U][kCopies];
+                bool on[U];
+                int64_t colb[U];
 #pragma unroll
-                for (int q = 0; q < kRowsPerWarp / 4; ++q) {
-                    const int r = row0 + rsub + 4 * q;
-                    int32_t v = -1;
-                    if (on) {
-                        if (stage_map) {
-                            v = mtile[r * a.K + k];
-                        } else {
-                            const int64_t row = tile * kTileM + r;
-                            v = row < a.n_out ? a.map[row * a.K + k] : -1;
+                for (int u = 0; u < U; ++u) {
+                    int image = -1, k0 = 0, c = 0;
+                    if (u0 + u < un.n) w.next(a, image, k0, c);
+                    const int k = k0 + (PACK > 1 ? slot : 0);
+                    const int bytes = PACK > 1 ? kSlotBytes : min(kRowBytes, a.row_bytes - c * kRowBytes);
+                    // chunks past a short last chunk are never read by the MMA; group members past
+                    // K are zero-stored (their weights are zero, but stale A bytes could be NaN)
+                    on[u] = image >= 0 && (PACK > 1 || j * 16 < bytes);
+                    colb[u] = PACK > 1 ? (int64_t)jj * 16 : (int64_t)c * kRowBytes + j * 16;
+#pragma unroll
+                    for (int q = 0; q < kCopies; ++q) {
+                        const int r = row0 + rsub + 4 * q;
+                        int32_t v = -1;
+                        if (on[u] && k < a.K) {
+                            if (stage_map) {
+                                v = mtile[r * a.K + k];
+                            } else {
+                                const int64_t row = tile * kTileM + r;
+                                v = row < a.n_out ? a.map[row * a.K + k] : -1;
+                            }
                         }
+                        src[u][q] = v;
                     }
-                    src[q] = v;
                 }
                 bool go = true;
                 if (lane == 0) go = mbar_wait(&empty[stage], phase ^ 1, abort);
@@ -242,13 +260,16 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                 }
                 const uint32_t As = smem_u32(smem + stage * kStage);
 #pragma unroll
-                for (int q = 0; q < kRowsPerWarp / 4; ++q) {
-                    if (!on) continue;
-                    const uint32_t dst = As + sw128_offset(row0 + rsub + 4 * q, j);
-                    if (src[q] >= 0 && src[q] < a.n_x)
-                        cp_async_16_hint(dst, a.x + (int64_t)src[q] * a.ldx_bytes + colb, 16u, keep);
-                    else
-                        st_shared_zero16(dst);
+                for (int u = 0; u < U; ++u) {
+                    if (!on[u]) continue;
+#pragma unroll
+                    for (int q = 0; q < kCopies; ++q) {
+                        const uint32_t dst = As + u * kABytes + sw128_offset(row0 + rsub + 4 * q, j);
+                        if (src[u][q] >= 0 && src[u][q] < a.n_x)
+                            cp_async_16_hint(dst, a.x + (int64_t)src[u][q] * a.ldx_bytes + colb[u], 16u, keep);
+                        else
+                            st_shared_zero16(dst);
+                    }
                 }
                 cp_async_commit();
                 ++it;
@@ -257,7 +278,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                     phase ^= 1;
                 }
                 if (it - sig > kLag) {
-                    // the copies of step `sig` have landed: publish them to the async proxy (tcgen05.mma)
+                    // the copies of stage `sig` have landed: publish them to the async proxy (tcgen05.mma)
                     cp_async_wait_group<kLag>();
                     fence_proxy_async();
                     __syncwarp();
@@ -269,7 +290,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
             __syncwarp();
             if (stage_map && lane == 0) mbar_arrive(&mempty[mb]);
             if (!ok) break;
-            mask_cur = mask_next;
         }
         cp_async_wait_group<0>();
         fence_proxy_async();
@@ -285,56 +305,45 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
         // addresses stay below 2^18, so the 14-bit start-address field never carries.
         if (lane == 0) {
             constexpr uint32_t idesc = EBYTES == 2 ? idesc_m128(BN, 1, 1) : idesc_m128(BN, 0, 0);
-            constexpr uint32_t kStageD = kStage >> 4, kBOffD = kABytes >> 4, kBTileD = kBTile >> 4,
-                               kSlotD = kSlotBytes >> 4;
+            constexpr uint32_t kStageD = kStage >> 4, kAD = kABytes >> 4, kBOffD = (U * kABytes) >> 4,
+                               kBTileD = kBTile >> 4;
             const uint64_t adesc0 = desc_sw128(smem_u32(smem));
-            const int last_k32 = (a.row_bytes - (a.nchunks - 1) * kRowBytes) >> 5;  // PACK == 1: last chunk
+            const int last_k32 = (a.row_bytes - (a.nchunks - 1) * kRowBytes) >> 5;  // pack == 1: last chunk
             uint32_t stage = 0, phase = 0;
             bool ok = true;
             int64_t tile = blockIdx.x;
-            uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
             for (int i = 0; tile < a.n_tiles && ok; tile += stride, ++i) {
-                const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
                 const int b = i & 1;
                 if (!mbar_wait(&tempty[b], ((i >> 1) & 1) ^ 1, abort)) break;
                 tc_fence_after();
                 const uint32_t d = tmem + b * BN;
-                const Steps st = make_steps(a, mask_cur);
+                const int n_units = tile_units<PACK>(a, tile).n;
                 uint32_t acc = 0;
                 int c = 0;
-                for (int s = 0; s < st.n_steps; ++s) {
+                for (int u0 = 0; u0 < n_units; u0 += U) {
                     if (!mbar_wait(&full[stage], phase, abort)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
                     const uint64_t ad = adesc0 + stage * kStageD, bd = ad + kBOffD;
-                    if (PACK > 1) {
-                        const int slots = min(PACK, st.n_act - s * PACK);
 #pragma unroll
-                        for (int p = 0; p < PACK; ++p) {
-                            if (p >= slots) break;
-#pragma unroll
-                            for (int h = 0; h < kSlotBytes / 32; ++h) {  // 32 bytes of K per MMA
-                                if (EBYTES == 2)
-                                    mma_f16(d, ad + p * kSlotD + 2 * h, bd + p * kBTileD + 2 * h, idesc, acc);
-                                else
-                                    mma_f8(d, ad + p * kSlotD + 2 * h, bd + p * kBTileD + 2 * h, idesc, acc);
-                                acc = 1;
-                            }
+                    for (int u = 0; u < U; ++u) {
+                        if (u0 + u >= n_units) break;
+                        int nk = 4;
+                        if (PACK == 1) {
+                            nk = c == a.nchunks - 1 ? last_k32 : 4;
+                            c = c + 1 == a.nchunks ? 0 : c + 1;
                         }
-                    } else {
-                        const int nk = c == a.nchunks - 1 ? last_k32 : 4;
 #pragma unroll
-                        for (int h = 0; h < 4; ++h) {
+                        for (int h = 0; h < 4; ++h) {  // 32 bytes of K per MMA
                             if (h >= nk) break;
                             if (EBYTES == 2)
-                                mma_f16(d, ad + 2 * h, bd + 2 * h, idesc, acc);
+                                mma_f16(d, ad + u * kAD + 2 * h, bd + u * kBTileD + 2 * h, idesc, acc);
                             else
-                                mma_f8(d, ad + 2 * h, bd + 2 * h, idesc, acc);
+                                mma_f8(d, ad + u * kAD + 2 * h, bd + u * kBTileD + 2 * h, idesc, acc);
                             acc = 1;
                         }
-                        c = c + 1 == a.nchunks ? 0 : c + 1;
                     }
                     mma_commit(&empty[stage]);
                     if (++stage == (uint32_t)S) {
@@ -347,7 +356,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                     mma_commit(&tfull[b]);
                 else
                     mbar_arrive(&tfull[b]);
-                mask_cur = mask_next;
             }
             // all issued MMAs complete before TMEM is released
             mma_commit(fin);
@@ -362,15 +370,13 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
         const int q4 = warp & 3;                           // TMEM lane quarter this warp may access
         const int rt = q4 * 32 + lane;                     // row of the tile this thread drains
         int64_t tile = blockIdx.x;
-        uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
         for (int i = 0; tile < a.n_tiles; tile += stride, ++i) {
-            const uint32_t mask_next = tile + stride < a.n_tiles ? load_mask(a, tile + stride) : 0;
             const int b = i & 1;
             const bool ready =
                 __all_sync(0xffffffffu, mbar_wait_backoff(&tfull[b], (i >> 1) & 1, abort, 128) && !*abort);
             if (!ready) break;
             tc_fence_after();
-            const Steps st = make_steps(a, mask_cur);
+            const int n_units = tile_units<PACK>(a, tile).n;
             const int64_t m0 = tile * kTileM;
             const int64_t left = a.n_out - m0;
             const int rows = left < kTileM ? (int)left : kTileM;
@@ -382,7 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 float v[16];
-                if (st.n_steps > 0) {
+                if (n_units > 0) {
                     tmem_ld16(tbase + c0, v);
                 } else {
 #pragma unroll
@@ -427,7 +433,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                     bulk_commit();
                 }
             }
-            mask_cur = mask_next;
         }
         if (a.direct_store && et == 0) bulk_wait<0>();
     } else {
@@ -440,36 +445,31 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                 mbar_arrive_expect_tx(&mfull[0], map_bytes);
                 bulk_g2s(smem_u32(map_sm), a.map + tile * kTileM * a.K, map_bytes, &mfull[0]);
             }
-            uint32_t mask_cur = tile < a.n_tiles ? load_mask(a, tile) : 0;
             for (int i = 0; tile < a.n_tiles && !*abort; tile += stride, ++i) {
                 const int64_t nxt = tile + stride;
-                const uint32_t mask_next = nxt < a.n_tiles ? load_mask(a, nxt) : 0;
                 if (stage_map && nxt < a.n_tiles) {
                     const int nb = (i + 1) & 1;
                     if (!mbar_wait_backoff(&mempty[nb], (((i + 1) >> 1) & 1) ^ 1, abort, 32)) break;
                     mbar_arrive_expect_tx(&mfull[nb], map_bytes);
                     bulk_g2s(smem_u32(map_sm + nb * map_words), a.map + nxt * kTileM * a.K, map_bytes, &mfull[nb]);
                 }
-                const Steps st = make_steps(a, mask_cur);
-                StepWalker w{st.kbits, 0, 0, -1};
+                const Units un = tile_units<PACK>(a, tile);
+                UnitWalker<PACK> w{un.bits, 0, 0, -1};
                 bool ok = true;
-                for (int s = 0; s < st.n_steps; ++s) {
-                    int ks[4], c;
-                    w.template next<PACK>(a, ks, c);
+                for (int u0 = 0; u0 < un.n; u0 += U) {
                     if (!mbar_wait(&empty[stage], phase ^ 1, abort)) {
                         ok = false;
                         break;
                     }
-                    int nb = 0;
+                    const int nu = min(U, un.n - u0);
+                    mbar_arrive_expect_tx(&full[stage], nu * kBTile);
+                    const uint32_t Bs = smem_u32(smem + stage * kStage) + U * kABytes;
 #pragma unroll
-                    for (int p = 0; p < PACK; ++p) nb += ks[p] >= 0 ? 1 : 0;
-                    mbar_arrive_expect_tx(&full[stage], nb * kBTile);
-                    const uint32_t Bs = smem_u32(smem + stage * kStage) + kABytes;
-#pragma unroll
-                    for (int p = 0; p < PACK; ++p) {
-                        if (ks[p] < 0) break;
-                        bulk_g2s(Bs + p * kBTile, a.wpack + ((int64_t)ks[p] * a.nchunks + c) * kBTile, kBTile,
-                                 &full[stage]);
+                    for (int u = 0; u < U; ++u) {
+                        if (u >= nu) break;
+                        int image, k0, c;
+                        w.next(a, image, k0, c);
+                        bulk_g2s(Bs + u * kBTile, a.wpack + (int64_t)image * kBTile, kBTile, &full[stage]);
                     }
                     if (++stage == (uint32_t)S) {
                         stage = 0;
@@ -477,7 +477,6 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                     }
                 }
                 if (!ok) break;
-                mask_cur = mask_next;
             }
         }
         __syncwarp();
@@ -491,26 +490,35 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
     if (threadIdx.x == 0 && *abort) atomicExch(a.err, FVGB_ETIMEOUT);
 }
 
-// Packed weight image: for every (k, chunk c): BN rows (output channel n) x 128 bytes holding
-// W[k][c*CE + e][n] for e in [0, CE) (CE = 128/ebytes), laid out exactly as the 128B-swizzled
-// K-major shared-memory operand (zero where c*CE+e >= cin or n >= cout).
+// Packed weight image: per unit one [BN rows (output channel n) x 128 bytes] block laid out
+// exactly as the 128B-swizzled K-major shared-memory operand.  pack == 1: unit (k, chunk c)
+// holds W[k][c*CE + e][n] for e in [0, CE) (CE = 128/ebytes); pack > 1: unit g holds
+// W[g*pack + p][e][n] at element p*cin + e of the row.  Zero where the channel, the offset or
+// n is out of range.
 __global__ void pack_weights_kernel(const uint8_t *__restrict__ w, int64_t K, int32_t cin, int32_t cout,
                                     int64_t wsk, int64_t wsci, int64_t wsco, int32_t ebytes, int32_t BN,
-                                    int32_t nchunks, uint8_t *__restrict__ out) {
-    const int64_t total = K * nchunks * BN * 128 / ebytes;  // elements of the image
+                                    int32_t nchunks, int32_t pack, int64_t units, uint8_t *__restrict__ out) {
     const int ce = 128 / ebytes;
+    const int64_t total = units * BN * ce;  // elements of the image
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t tilei = e / ((int64_t)BN * ce);
         const int64_t rem = e % ((int64_t)BN * ce);
         const int n = (int)(rem / ce), kk = (int)(rem % ce);
-        const int64_t k = tilei / nchunks;
-        const int c = (int)(tilei % nchunks);
-        const int ci = c * ce + kk;
+        int64_t k;
+        int ci;
+        if (pack > 1) {
+            const int p = kk / cin;
+            k = tilei * pack + p;
+            ci = kk - p * cin;
+        } else {
+            k = tilei / nchunks;
+            ci = (int)(tilei % nchunks) * ce + kk;
+        }
         const uint32_t byte = (uint32_t)kk * ebytes;
         const uint32_t off = sw128_offset((uint32_t)n, byte >> 4) + (byte & 15);
         uint8_t *dst = out + tilei * (int64_t)BN * 128 + off;
-        const bool ok = ci < cin && n < cout;
-        const int64_t src = (k * wsk + (int64_t)ci * wsci + (int64_t)n * wsco) * ebytes;
+        const bool ok = k < K && ci < cin && n < cout;
+        const int64_t src = ok ? (k * wsk + (int64_t)ci * wsci + (int64_t)n * wsco) * ebytes : 0;
         if (ebytes == 2) {
             *reinterpret_cast<uint16_t *>(dst) = ok ? *reinterpret_cast<const uint16_t *>(w + src) : (uint16_t)0;
         } else {
@@ -525,6 +533,13 @@ int tile_n(int32_t cout) {
     if (cout <= 128) return 128;
     if (cout <= 256) return 256;
     return -1;
+}
+
+// Units of the packed weight image for (K, c_in*elem bytes).
+int64_t weight_units(int64_t K, int64_t row_bytes, int *pack, int *nchunks) {
+    *pack = row_bytes < 128 ? (int)(128 / row_bytes) : 1;
+    *nchunks = (int)ceil_div(row_bytes, 128);
+    return *pack > 1 ? ceil_div(K, (int64_t)*pack) : K * *nchunks;
 }
 
 int sm_count() {
@@ -543,17 +558,19 @@ int sm_count() {
 
 template <int BN, int EB, int PACK>
 int launch_fwd(FwdArgs a, cudaStream_t s) {
-    const int stage = kABytes + PACK * BN * kRowBytes;
+    // two units per stage where both fit next to a deep enough ring; one for wide outputs
+    constexpr int U = BN <= 64 ? 2 : 1;
+    constexpr int stage = U * (kABytes + BN * kRowBytes);
     const int map_bytes = a.K <= kMaxMapStage ? 2 * kTileM * a.K * 4 : 0;
     a.direct_store = (a.direct_store && BN <= 128) ? 1 : 0;  // staging tile only where it fits
     const int fixed = 1024 + map_bytes + (a.direct_store ? kTileM * BN * 2 : 0) + (2 * 8 + 9) * 8 + 16;
     int stages = 8;
     while (stages > kLag + 1 && stages * stage + fixed > 227 * 1024) --stages;
-    // a gather thread publishes a stage kLag steps late, so the ring needs more than kLag stages
+    // a gather thread publishes a stage kLag stages late, so the ring needs more than kLag stages
     if (stages < kLag + 1 || stages * stage + fixed > 227 * 1024) return FVGB_EINVAL;
     a.stages = stages;
     const int smem = stages * stage + fixed;
-    auto kern = conv_tc_fwd_kernel<BN, EB, PACK>;
+    auto kern = conv_tc_fwd_kernel<BN, EB, PACK, U>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
         return launch_status();
     const int64_t grid = std::min<int64_t>(a.n_tiles, sm_count());
@@ -596,8 +613,8 @@ extern "C" int fvgb_tc_weight_bytes(int32_t dtype, int64_t K, int32_t cin, int32
     if (!eb) return FVGB_ETYPE;
     const int BN = tile_n(cout);
     if (BN < 0) return FVGB_EINVAL;
-    const int64_t nchunks = ceil_div((int64_t)cin * eb, 128);
-    *bytes = (size_t)(K * nchunks * BN * 128);
+    int pack = 1, nchunks = 1;
+    *bytes = (size_t)(weight_units(K, (int64_t)cin * eb, &pack, &nchunks) * BN * 128);
     return FVGB_OK;
 }
 
@@ -610,11 +627,12 @@ extern "C" int fvgb_tc_pack_weights(int32_t dtype, const void *w, int64_t K, int
     if (!w || !packed || packed_bytes < need) return FVGB_EINVAL;
     const int eb = dtype == FVGB_E4M3 ? 1 : 2;
     const int BN = tile_n(cout);
-    const int nchunks = (int)ceil_div((int64_t)cin * eb, 128);
+    int pack = 1, nchunks = 1;
+    const int64_t units = weight_units(K, (int64_t)cin * eb, &pack, &nchunks);
     const int64_t total = (int64_t)need / eb;
     const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(total, 256), 4096);
     pack_weights_kernel<<<blocks, 256, 0, as_stream(stream)>>>((const uint8_t *)w, K, cin, cout, wsk, wsci, wsco, eb, BN,
-                                                               nchunks, (uint8_t *)packed);
+                                                               nchunks, pack, units, (uint8_t *)packed);
     count_launches(1);
     return launch_status();
 }
@@ -647,9 +665,13 @@ extern "C" int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32
     a.K = K;
     a.tile_mask = tile_mask;
     a.wpack = (const uint8_t *)packed_w;
-    a.nchunks = (int32_t)ceil_div(row_bytes, 128);
-    a.pack = row_bytes < 128 ? (int32_t)(128 / row_bytes) : 1;
-    if (a.pack > 4) return FVGB_EINVAL;
+    int pack = 1, nchunks = 1;
+    weight_units(K, row_bytes, &pack, &nchunks);
+    if (pack > 4) return FVGB_EINVAL;
+    a.nchunks = nchunks;
+    a.pack = pack;
+    a.groups = (int32_t)ceil_div((int64_t)K, (int64_t)pack);
+    // the group bit set of a K <= 32 mask has at most 16 bits; K > 32 walks units linearly
     a.row_bytes = (int32_t)row_bytes;
     a.cout = c_out;
     a.y = (uint8_t *)y;

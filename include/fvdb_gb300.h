@@ -267,9 +267,11 @@ int fvgb_tc_weight_bytes(int32_t dtype, int64_t K, int32_t c_in, int32_t c_out, 
 
 /*
  * Pack W (element (k, ci, co) at w[k*wsk + ci*wsci + co*wsco], elements of `dtype`) into
- * the tile image of fvgb_conv_fwd_tc: per (offset, 128-byte channel chunk) one
- * [N_tile x 128 B] block in the 128B-swizzled K-major shared-memory layout, zero padded.
- * Strides select W or W^T, so the same image format serves forward and data gradient.
+ * the tile image of fvgb_conv_fwd_tc: one [N_tile x 128 B] block per 128-byte unit of the
+ * reduction, in the 128B-swizzled K-major shared-memory layout, zero padded.  A unit is one
+ * (offset, 128-byte channel chunk) when c_in*elem >= 128 bytes, else a group of
+ * 128/(c_in*elem) consecutive offsets side by side.  Strides select W or W^T, so the same
+ * image format serves forward and data gradient.
  */
 int fvgb_tc_pack_weights(int32_t dtype, const void *w, int64_t K, int32_t c_in, int32_t c_out, int64_t wsk,
                          int64_t wsci, int64_t wsco, void *packed, size_t packed_bytes, fvgb_stream_t stream);
