@@ -146,6 +146,54 @@ def useful_flops(p1, p2, cin1=32, cout1=64, cin2=64, cout2=64) -> tuple[float, i
     return 2.0 * (P1 * cin1 * cout1 + P2 * cin2 * cout2), P1, P2
 
 
+# DRAM bytes (read + write) of one layer-1 contraction launch per voxel, from the ncu capture
+# summarised in profiles/conv_tc_fwd_l1_830k_full.md: (142.95 + 70.46) MB over 829,865 voxels
+# of the same workload generator at 500k points per grid; traffic grows with the voxel count.
+L1_DRAM_BYTES_PER_VOXEL = (142.949e6 + 70.459e6) / 829_865
+
+
+def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) -> tuple[float, bool]:
+    """Layer-1 tcgen05 contraction alone through the C ABI (fvgb_conv_fwd_tc): average launch
+    duration from CUDA events around `launches` back-to-back launches on the current stream,
+    and whether its output is bitwise identical to the same layer run through
+    SparseConvPackInfo.sparse_conv_3d."""
+    import ctypes
+
+    n = x.shape[0]
+    kmap = p1._impl.kmap()  # [rows padded to 128, K] int32, -1 = absent
+    tm = p1._impl.tile_mask(False)
+    K = kmap.shape[1]
+    cout, cin = w1.shape[0], w1.shape[1]
+    wkio = w1.permute(4, 3, 2, 1, 0).reshape(K, cin, cout).contiguous()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    nb = ctypes.c_size_t(0)
+    assert lib.fvgb_tc_weight_bytes(2, ctypes.c_int64(K), cin, cout, ctypes.byref(nb)) == 0
+    packed = torch.empty(nb.value, dtype=torch.uint8, device=x.device)
+    assert lib.fvgb_tc_pack_weights(2, P(wkio), ctypes.c_int64(K), cin, cout, ctypes.c_int64(cin * cout),
+                                    ctypes.c_int64(cout), ctypes.c_int64(1), P(packed), nb, stream) == 0
+    y = torch.empty(n, cout, device=x.device, dtype=torch.bfloat16)
+    err = torch.zeros(1, dtype=torch.int32, device=x.device)
+
+    def launch():
+        rc = lib.fvgb_conv_fwd_tc(2, P(x), ctypes.c_int64(n), cin, ctypes.c_int64(x.stride(0)), P(kmap),
+                                  ctypes.c_int64(n), K, P(tm) if tm is not None else None, P(packed), cout, P(y),
+                                  ctypes.c_int64(cout), None, P(err), stream)
+        assert rc == 0, rc
+
+    launch()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(launches):
+        launch()
+    b.record()
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    identical = bool(torch.equal(p1.sparse_conv_3d(x, w1).jdata, y))
+    return a.elapsed_time(b) / launches, identical
+
+
 def load_peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -311,6 +359,7 @@ def run_gpu(args) -> None:
         torch.cuda.synchronize()
         e2e_ms = t0.elapsed_time(t1) / e2e_steps
 
+    kern_ms, kern_identical = kernel_only_l1(lib, p1, x, model.w1, max(args.steps, 3))
     peaks = load_peaks()
     conv1_flops = 2.0 * P1 * 32 * 64
     conv1_bytes = n_vox * 32 * 2 + n_vox * 64 * 2 + 27 * 32 * 64 * 2 + 4 * 27 * n_vox
@@ -336,16 +385,20 @@ def run_gpu(args) -> None:
         "gpu_launches": int(l1 - l0),
         "clocks": clk,
         "roofline": {
-            "kernel": "layer-1 contraction (3^3 32->64)",
+            "kernel": "conv_tc_fwd_kernel, layer-1 contraction (3^3 32->64)",
             "bound": "hbm",
-            "achieved": conv1_bytes / (conv_ms * 1e-3) / 1e9,
+            "achieved": conv1_bytes / (kern_ms * 1e-3) / 1e9,
             "peak": peaks["hbm_gbs"],
             "unit": "GB/s",
-            "frac": conv1_bytes / (conv_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
-            "traffic": None,
+            "frac": conv1_bytes / (kern_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
+            "traffic": L1_DRAM_BYTES_PER_VOXEL * n_vox,
+            "algorithmic_bytes": conv1_bytes,
             "peak_source": peaks["src"],
-            "kernel_ms": conv_ms,
-            "kernel_tflops": conv1_flops / (conv_ms * 1e-3) / 1e12,
+            "kernel_ms": kern_ms,
+            "kernel_output_identical_to_step": kern_identical,
+            "kernel_tflops": conv1_flops / (kern_ms * 1e-3) / 1e12,
+            "tensor_frac": conv1_flops / (kern_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
+            "layer1_window_ms": conv_ms,
         },
     }
     if rank == 0 and not args.no_cpu_baseline:

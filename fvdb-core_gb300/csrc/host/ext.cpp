@@ -711,6 +711,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
              py::arg("kernel_size"), py::arg("stride"), py::arg("source_grid"), py::arg("target_grid") = py::none())
         .def("kmap", [](PackPtr p) { return pack_kmap(p); })
         .def("kmap_t", [](PackPtr p) { return pack_kmap_t(p); })
+        .def("tile_mask", [](PackPtr p, bool transposed) { return pack_tile_mask(p, transposed); },
+             py::arg("transposed") = false)
         .def("build_gather_scatter", &pack_build_gather_scatter)
         .def("build_implicit_gemm", &pack_build_implicit_gemm)
         .def_property_readonly("kernel_size", [](const PackInfo &p) { return py::make_tuple(p.ks.v[0], p.ks.v[1], p.ks.v[2]); })
