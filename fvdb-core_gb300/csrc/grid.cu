@@ -53,15 +53,51 @@ size_t sort_ws_layout(int64_t n, SortWs *ws, char *base) {
     return off;
 }
 
+// box_lo/box_hi: bounds every coordinate must lie in (the whole coordinate range when the
+// caller promises none); a coordinate outside raises FVGB_ERANGE.
 __global__ void keys_kernel(const int32_t *__restrict__ ijk, const int64_t *__restrict__ joff,
-                            int32_t B, int64_t n, uint64_t *__restrict__ keys,
+                            int32_t B, int64_t n, int3 box_lo, int3 box_hi, uint64_t *__restrict__ keys,
                             int32_t *__restrict__ bidx, int32_t *__restrict__ err) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int32_t x = ijk[3 * i], y = ijk[3 * i + 1], z = ijk[3 * i + 2];
-    if (!coord_in_range(x) || !coord_in_range(y) || !coord_in_range(z)) atomicExch(err, FVGB_ERANGE);
+    if (!coord_in_range(x) || !coord_in_range(y) || !coord_in_range(z) || x < box_lo.x || x > box_hi.x ||
+        y < box_lo.y || y > box_hi.y || z < box_lo.z || z > box_hi.z)
+        atomicExch(err, FVGB_ERANGE);
     keys[i] = order_key(x, y, z);
     bidx[i] = batch_of(joff, B, i);
+}
+
+// One past the highest order_key bit that can differ between coordinates in [lo, hi] (per
+// axis): coordinate bits above the highest bit where lo and hi differ are shared by the whole
+// box.  Coordinate bit c of x lands on key bit 6+c (leaf), 14+c (lower node), 24+c (upper node)
+// or 42+c (root); y sits 3, 4, 5 or 9 positions below x in those fields and z twice as far.
+// Within an axis a higher coordinate bit always maps to a higher key bit, so all keys of the
+// box agree above the returned bit and sorting only the bits below it orders them exactly as a
+// full 63-bit sort.
+int order_key_end_bit(const int32_t lo[3], const int32_t hi[3]) {
+    static const int kBase[3] = {6, 3, 0};  // x, y, z offset of the leaf field
+    int end = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (lo[a] > hi[a]) continue;
+        const uint32_t d = (uint32_t)lo[a] ^ (uint32_t)hi[a];
+        if (!d) continue;
+        int h = 31;
+        while (!((d >> h) & 1u)) --h;
+        int kb;
+        if (h < 3)
+            kb = kBase[a] + h;                    // leaf: bits 0..8
+        else if (h < 7)
+            kb = 9 + 4 * (2 - a) + (h - 3);       // lower node: x 17..20, y 13..16, z 9..12
+        else if (h < 12)
+            kb = 21 + 5 * (2 - a) + (h - 7);      // upper node: x 31..35, y 26..30, z 21..25
+        else if (h < 21)
+            kb = 36 + 9 * (2 - a) + (h - 12);     // root: x 54..62, y 45..53, z 36..44
+        else
+            return 63;
+        if (kb + 1 > end) end = kb + 1;
+    }
+    return end;
 }
 
 __global__ void unique_flags_kernel(const uint64_t *__restrict__ keys,
@@ -254,10 +290,11 @@ extern "C" int fvgb_ijk_sort_unique_workspace(int64_t n, int32_t num_grids, size
     return FVGB_OK;
 }
 
-extern "C" int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids,
-                                    int64_t n, int32_t *out_ijk, int64_t *out_joffsets,
-                                    int32_t *err_dev, void *workspace, size_t workspace_bytes,
-                                    fvgb_stream_t stream) {
+namespace fvgb {
+namespace {
+int sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids, int64_t n, const int32_t *box_lo,
+                const int32_t *box_hi, int32_t *out_ijk, int64_t *out_joffsets, int32_t *err_dev, void *workspace,
+                size_t workspace_bytes, fvgb_stream_t stream) {
     if (n < 0 || num_grids < 1 || !joffsets || !out_joffsets || !err_dev) return FVGB_EINVAL;
     if (n > 0 && (!ijk || !out_ijk)) return FVGB_EINVAL;
     if (n >= (int64_t)INT32_MAX) return FVGB_EINVAL;
@@ -271,11 +308,20 @@ extern "C" int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets,
             return launch_status();
         return launch_status();
     }
-    keys_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, joffsets, num_grids, n, w.keys_a, w.bidx_a, err_dev);
+    int3 lo = make_int3(INT32_MIN, INT32_MIN, INT32_MIN), hi = make_int3(INT32_MAX, INT32_MAX, INT32_MAX);
+    int end_bit = 63;
+    if (box_lo && box_hi) {
+        for (int a = 0; a < 3; ++a)
+            if (box_lo[a] > box_hi[a]) return FVGB_EINVAL;
+        lo = make_int3(box_lo[0], box_lo[1], box_lo[2]);
+        hi = make_int3(box_hi[0], box_hi[1], box_hi[2]);
+        end_bit = order_key_end_bit(box_lo, box_hi);
+    }
+    keys_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, joffsets, num_grids, n, lo, hi, w.keys_a, w.bidx_a, err_dev);
     size_t tb = w.cub_bytes;
-    // 1) sort by voxel key (stable radix), 2) stable sort by grid index: grids stay
-    //    contiguous and every grid's voxels stay in key order.
-    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.bidx_a, w.bidx_b, n, 0, 63, s);
+    // 1) sort by voxel key (stable radix, only the bits that can differ), 2) stable sort by grid
+    //    index: grids stay contiguous and every grid's voxels stay in key order.
+    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.bidx_a, w.bidx_b, n, 0, end_bit, s);
     const uint64_t *keys = w.keys_b;
     const int32_t *bidx = w.bidx_b;
     if (num_grids > 1) {
@@ -296,6 +342,25 @@ extern "C" int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets,
                                                                                     out_joffsets);
     count_launches(4);
     return launch_status();
+}
+}  // namespace
+}  // namespace fvgb
+
+extern "C" int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids,
+                                    int64_t n, int32_t *out_ijk, int64_t *out_joffsets,
+                                    int32_t *err_dev, void *workspace, size_t workspace_bytes,
+                                    fvgb_stream_t stream) {
+    return fvgb::sort_unique(ijk, joffsets, num_grids, n, nullptr, nullptr, out_ijk, out_joffsets, err_dev,
+                             workspace, workspace_bytes, stream);
+}
+
+extern "C" int fvgb_ijk_sort_unique_in_box(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids,
+                                           int64_t n, const int32_t *box_lo, const int32_t *box_hi,
+                                           int32_t *out_ijk, int64_t *out_joffsets, int32_t *err_dev,
+                                           void *workspace, size_t workspace_bytes, fvgb_stream_t stream) {
+    if (!box_lo || !box_hi) return FVGB_EINVAL;
+    return fvgb::sort_unique(ijk, joffsets, num_grids, n, box_lo, box_hi, out_ijk, out_joffsets, err_dev,
+                             workspace, workspace_bytes, stream);
 }
 
 extern "C" int fvgb_scan_workspace(int64_t n, size_t *bytes) {

@@ -44,6 +44,24 @@ Tensor workspace(size_t bytes, const torch::Device &dev) {
     return torch::empty({(int64_t)std::max<size_t>(bytes, 256)}, torch::dtype(torch::kUInt8).device(dev));
 }
 
+// Pinned host staging for the small device-to-host reads of grid builds (per device, grown on
+// demand): one async copy and one stream sync instead of a torch gather + copy.
+int64_t *pinned_meta(int dev, size_t count) {
+    static std::mutex mu;
+    static std::vector<std::pair<int64_t *, size_t>> bufs(64, {nullptr, 0});
+    std::lock_guard<std::mutex> lock(mu);
+    auto &b = bufs.at(dev);
+    if (b.second < count) {
+        if (b.first) cudaFreeHost(b.first);
+        const size_t cap = std::max<size_t>(count, 512);
+        void *p = nullptr;
+        TORCH_CHECK(cudaHostAlloc(&p, cap * sizeof(int64_t), cudaHostAllocDefault) == cudaSuccess,
+                    "pinned staging allocation failed");
+        b = {reinterpret_cast<int64_t *>(p), cap};
+    }
+    return b.first;
+}
+
 int64_t next_pow2(int64_t v) {
     int64_t p = 64;
     while (p < v) p <<= 1;
@@ -72,6 +90,7 @@ struct GridImpl {
     Tensor voxel_sizes;    // float64 [B,3] cpu
     Tensor origins;        // float64 [B,3] cpu
     Tensor jidx_cache;
+    int32_t box_lo[3] = {0, 0, 0}, box_hi[3] = {-1, -1, -1};  // bounding box of ijk (empty if N == 0)
 
     FvgbGrid view() const {
         FvgbGrid g;
@@ -98,8 +117,11 @@ Tensor per_grid_vec(const Tensor &t, int64_t B, const char *name) {
     return v.contiguous().clone();
 }
 
-// Sorted-unique voxels in index order + leaf table + hash (one host sync for the counts).
-GridPtr build_grid(const Tensor &ijk_in, const Tensor &joff_in, const Tensor &vs, const Tensor &org) {
+// Sorted-unique voxels in index order + leaf table + hash (one host sync for the counts and the
+// bounding box).  box_lo/box_hi (optional): bounds the caller knows for ijk, which shorten the
+// sort to the order-key bits that can differ.
+GridPtr build_grid(const Tensor &ijk_in, const Tensor &joff_in, const Tensor &vs, const Tensor &org,
+                   const int32_t *box_lo = nullptr, const int32_t *box_hi = nullptr) {
     TORCH_CHECK(ijk_in.is_cuda(), "fvdb_gb300 grids live on CUDA devices");
     c10::cuda::CUDAGuard guard(ijk_in.device());
     auto dev = ijk_in.device();
@@ -116,31 +138,59 @@ GridPtr build_grid(const Tensor &ijk_in, const Tensor &joff_in, const Tensor &vs
     g->origins = per_grid_vec(org, B, "origins");
     auto i32 = torch::dtype(torch::kInt32).device(dev);
     Tensor out_ijk = torch::empty({std::max<int64_t>(n, 1), 3}, i32);
-    Tensor out_joff = torch::empty({B + 1}, torch::dtype(torch::kInt64).device(dev));
-    Tensor err = torch::zeros({1}, i32);
+    // device metadata read back in one copy: [0, B] voxel offsets, B+1 leaf count, B+2 voxel
+    // count, B+3 error word (the sort's int32 flag in its low half; zero-initialised), then the
+    // measured bounding box (lo xyz, hi xyz) when the caller gave none
+    const int64_t n_meta = B + 4 + ((box_lo && box_hi) ? 0 : 6);
+    Tensor meta = torch::zeros({n_meta}, torch::dtype(torch::kInt64).device(dev));
+    Tensor out_joff = meta.narrow(0, 0, B + 1);
+    int32_t *err_ptr = reinterpret_cast<int32_t *>(meta.data_ptr<int64_t>() + B + 3);
+    static_assert(sizeof(void *) == 8, "64-bit host");
     size_t wsb = 0;
     check_status(fvgb_ijk_sort_unique_workspace(n, (int32_t)B, &wsb), "grid build (workspace)");
     Tensor ws = workspace(wsb, dev);
     auto s = cur_stream();
-    check_status(fvgb_ijk_sort_unique(n ? ijk.data_ptr<int32_t>() : nullptr, joff.data_ptr<int64_t>(), (int32_t)B,
-                                      n, out_ijk.data_ptr<int32_t>(), out_joff.data_ptr<int64_t>(),
-                                      err.data_ptr<int32_t>(), ws.data_ptr(), ws.numel(), s),
-                 "grid build (sort)");
+    if (box_lo && box_hi)
+        check_status(fvgb_ijk_sort_unique_in_box(n ? ijk.data_ptr<int32_t>() : nullptr, joff.data_ptr<int64_t>(),
+                                                 (int32_t)B, n, box_lo, box_hi, out_ijk.data_ptr<int32_t>(),
+                                                 out_joff.data_ptr<int64_t>(), err_ptr, ws.data_ptr(), ws.numel(), s),
+                     "grid build (sort)");
+    else
+        check_status(fvgb_ijk_sort_unique(n ? ijk.data_ptr<int32_t>() : nullptr, joff.data_ptr<int64_t>(), (int32_t)B,
+                                          n, out_ijk.data_ptr<int32_t>(), out_joff.data_ptr<int64_t>(), err_ptr,
+                                          ws.data_ptr(), ws.numel(), s),
+                     "grid build (sort)");
     // leaf ids over the capacity n (the unique count stays on the device), so the unique count,
     // the leaf count and the range check come back to the host in one copy
     Tensor leaf_ids = torch::empty({std::max<int64_t>(n, 1)}, i32);
-    Tensor counts = torch::zeros({2}, torch::dtype(torch::kInt64).device(dev));
     size_t sb = 0;
     check_status(fvgb_scan_workspace(n, &sb), "grid build (scan workspace)");
-    Tensor ws2 = workspace(sb, dev);
+    // the sort's workspace is free again: reuse it for the leaf scan when large enough
+    Tensor ws2 = sb <= (size_t)ws.numel() ? ws : workspace(sb, dev);
     check_status(fvgb_grid_leaf_scan(n ? out_ijk.data_ptr<int32_t>() : nullptr, out_joff.data_ptr<int64_t>(), (int32_t)B,
-                                     n, leaf_ids.data_ptr<int32_t>(), counts.data_ptr<int64_t>(), ws2.data_ptr(),
+                                     n, leaf_ids.data_ptr<int32_t>(), meta.data_ptr<int64_t>() + B + 1, ws2.data_ptr(),
                                      ws2.numel(), s),
                  "grid build (leaf scan)");
-    Tensor host = torch::cat({out_joff, counts, err.to(torch::kInt64)}).cpu();
-    const int64_t *h = host.data_ptr<int64_t>();
-    TORCH_CHECK_VALUE(h[B + 3] == 0, "voxel coordinates must lie in [-2^20, 2^20)");
-    g->joffsets_host = host.narrow(0, 0, B + 1).contiguous();
+    if (!(box_lo && box_hi) && n > 0)  // the bounding box of the input is that of the unique voxels
+        meta.narrow(0, B + 4, 6).copy_(torch::cat({std::get<0>(ijk.min(0)), std::get<0>(ijk.max(0))}));
+    int64_t *h = pinned_meta(dev.index(), (size_t)n_meta);
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(s);
+    TORCH_CHECK(cudaMemcpyAsync(h, meta.data_ptr<int64_t>(), n_meta * sizeof(int64_t), cudaMemcpyDeviceToHost, cs) ==
+                        cudaSuccess &&
+                    cudaStreamSynchronize(cs) == cudaSuccess,
+                "grid build: reading the counts failed");
+    TORCH_CHECK_VALUE(h[B + 3] == 0, box_lo ? "voxel coordinates must lie in [-2^20, 2^20) and inside their bounds"
+                                            : "voxel coordinates must lie in [-2^20, 2^20)");
+    for (int a = 0; a < 3; ++a) {
+        if (box_lo && box_hi) {
+            g->box_lo[a] = box_lo[a];
+            g->box_hi[a] = box_hi[a];
+        } else if (n > 0) {
+            g->box_lo[a] = (int32_t)h[B + 4 + a];
+            g->box_hi[a] = (int32_t)h[B + 7 + a];
+        }
+    }
+    g->joffsets_host = torch::from_blob(h, {B + 1}, torch::kInt64).clone();
     g->joffsets = out_joff;
     g->N = h[B];
     g->ijk = out_ijk.narrow(0, 0, g->N);
@@ -215,7 +265,23 @@ GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, cons
         const int64_t m = joff[g->B].item<int64_t>();
         ijk = out.narrow(0, 0, m);
     }
-    return build_grid(ijk, joff, g->voxel_sizes, g->origins);
+    // bounds of the candidates from the source grid's bounding box: floor(ijk/s) per axis on the
+    // coarse path; (ijk + offset)/s over the footprint otherwise (k0 and s0 act on axis 2)
+    if (g->N == 0) return build_grid(ijk, joff, g->voxel_sizes, g->origins);
+    auto fdiv = [](int64_t a, int64_t b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
+    int32_t lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        if (coarse) {
+            lo[a] = (int32_t)fdiv(g->box_lo[a], st.v[a]);
+            hi[a] = (int32_t)fdiv(g->box_hi[a], st.v[a]);
+        } else {
+            const int64_t k = ks.v[2 - a], s = st.v[2 - a];
+            const int64_t dlo = k % 2 == 0 ? 0 : -(k - 1) / 2, dhi = k % 2 == 0 ? k - 1 : (k - 1) / 2;
+            lo[a] = (int32_t)fdiv(g->box_lo[a] + dlo, s);
+            hi[a] = (int32_t)fdiv(g->box_hi[a] + dhi, s);
+        }
+    }
+    return build_grid(ijk, joff, g->voxel_sizes, g->origins, lo, hi);
 }
 
 Tensor grid_ijk_to_index(const GridPtr &g, const Tensor &ijk_in, const Tensor &joff_in, bool cumulative) {

@@ -105,6 +105,19 @@ int fvgb_ijk_sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t nu
                          size_t workspace_bytes, fvgb_stream_t stream);
 
 /*
+ * fvgb_ijk_sort_unique for callers that know bounds of the coordinates: every ijk lies in
+ * [box_lo, box_hi] (host int32[3] each).  The radix sort then covers only the order-key bits
+ * that can differ inside the box (e.g. 21 of 63 bits for coordinates in [0,128)^3), with the
+ * same result as the full sort; a coordinate outside the box raises FVGB_ERANGE in *err_dev.
+ * Same workspace as fvgb_ijk_sort_unique.  Used for conv_grid targets, whose bounds follow
+ * from the source grid's (no counterpart in the reference: its builder sorts full keys).
+ */
+int fvgb_ijk_sort_unique_in_box(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids, int64_t n,
+                                const int32_t *box_lo, const int32_t *box_hi, int32_t *out_ijk,
+                                int64_t *out_joffsets, int32_t *err_dev, void *workspace,
+                                size_t workspace_bytes, fvgb_stream_t stream);
+
+/*
  * Leaf ids of sorted unique ijk: leaf_ids[i] = 1 + id of the leaf of voxel i (inclusive scan
  * of leaf starts).  n is a capacity (>= joffsets[num_grids], the voxel count, read on the
  * device), so this can run straight after fvgb_ijk_sort_unique without a host round trip.

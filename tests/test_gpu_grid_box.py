@@ -1,0 +1,65 @@
+"""fvgb_ijk_sort_unique_in_box: sorting only the order-key bits that can differ inside known
+coordinate bounds gives exactly the full sort's voxels and offsets; a coordinate outside the
+bounds is reported as FVGB_ERANGE."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+FVGB_ERANGE = 3
+
+
+def _sort(lib, ijk, joff, box):
+    n, B = ijk.shape[0], joff.numel() - 1
+    wb = ctypes.c_size_t(0)
+    assert lib.fvgb_ijk_sort_unique_workspace(ctypes.c_int64(n), ctypes.c_int32(B), ctypes.byref(wb)) == 0
+    ws = torch.empty(wb.value, dtype=torch.uint8, device=ijk.device)
+    out = torch.empty_like(ijk)
+    ooff = torch.empty(B + 1, dtype=torch.int64, device=ijk.device)
+    err = torch.zeros(1, dtype=torch.int32, device=ijk.device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    if box is None:
+        rc = lib.fvgb_ijk_sort_unique(P(ijk), P(joff), ctypes.c_int32(B), ctypes.c_int64(n), P(out), P(ooff), P(err),
+                                      P(ws), wb, stream)
+    else:
+        lo, hi = (ctypes.c_int32 * 3)(*box[0]), (ctypes.c_int32 * 3)(*box[1])
+        rc = lib.fvgb_ijk_sort_unique_in_box(P(ijk), P(joff), ctypes.c_int32(B), ctypes.c_int64(n), lo, hi, P(out),
+                                             P(ooff), P(err), P(ws), wb, stream)
+    assert rc == 0
+    torch.cuda.synchronize()
+    m = int(ooff[-1].item())
+    return out[:m].cpu(), ooff.cpu(), int(err.item())
+
+
+@pytest.mark.parametrize("lo,hi", [((0, 0, 0), (127, 127, 127)), ((-300, 1000, -5000), (500, 1040, -4000)),
+                                   ((7, -9, 4095), (7, 9, 4100)), ((-2**20, 0, 0), (2**20 - 1, 3, 5)),
+                                   ((3, 3, 3), (3, 3, 3))])
+def test_bounded_sort_equals_full_sort(cuda_device, lo, hi):
+    from fvdb import _lib
+
+    lib = _lib.cdll()
+    rng = np.random.default_rng(abs(hash((lo, hi))) % 2**32)
+    n = 60000
+    ijk = np.stack([rng.integers(lo[a], hi[a] + 1, n) for a in range(3)], 1).astype(np.int32)
+    ijk_d = torch.from_numpy(ijk).to(cuda_device)
+    joff = torch.tensor([0, n // 3, n], dtype=torch.int64, device=cuda_device)
+    full = _sort(lib, ijk_d, joff, None)
+    boxed = _sort(lib, ijk_d, joff, (lo, hi))
+    assert full[2] == 0 and boxed[2] == 0
+    assert torch.equal(full[0], boxed[0])
+    assert torch.equal(full[1], boxed[1])
+
+
+def test_coordinate_outside_box_is_reported(cuda_device):
+    from fvdb import _lib
+
+    lib = _lib.cdll()
+    ijk = torch.tensor([[0, 0, 0], [5, 5, 5], [9, 2, 2]], dtype=torch.int32, device=cuda_device)
+    joff = torch.tensor([0, 3], dtype=torch.int64, device=cuda_device)
+    assert _sort(lib, ijk, joff, ((0, 0, 0), (8, 8, 8)))[2] == FVGB_ERANGE
+    assert _sort(lib, ijk, joff, ((0, 0, 0), (9, 8, 8)))[2] == 0
