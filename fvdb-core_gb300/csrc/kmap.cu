@@ -179,6 +179,142 @@ __global__ void __launch_bounds__(kKmapThreads) kmap_leaf_kernel(KmapParams p) {
     }
 }
 
+constexpr int kWarpLeaves = 4;      // target leaves (one per warp) per CTA
+constexpr int kMaxWindowWarp = 64;  // source leaves a warp stages
+
+// One warp per target leaf, four per CTA, with warp-private shared memory and no CTA-wide
+// barrier: a leaf has ~50 active voxels on surface grids, so a whole CTA per leaf idles most of
+// its threads at barriers while one warp resolves the window.  Each warp stages its source-leaf
+// window (one hash probe per lane), ranks the target leaf's active slots (16 per lane), then
+// builds 32 rows at a time, one lane per row: the row's window-local coordinates are computed
+// once and the three offset components are walked as nested loops, so an entry costs a
+// window-leaf lookup, one mask-word test and a popcount.  Rows are assembled in shared memory
+// (odd row stride: no bank conflicts) and written out coalesced.
+// Per-warp shared memory: WinLeaf[window] | uint16 slots[512] | int32 rows[32][K|1] |
+//                         uint32 tmask[8] | int32 counts[K] (nbsizes only)
+// KS > 0: cubic KS^3 kernel (loops unrolled at compile time); KS == 0: any kernel size.
+template <int KS>
+__global__ void __launch_bounds__(32 * kWarpLeaves) kmap_warp_kernel(KmapParams p, int32_t warp_bytes) {
+    extern __shared__ __align__(16) uint8_t kmap_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t leaf_id = (int64_t)blockIdx.x * kWarpLeaves + warp;
+    if (leaf_id >= p.tgt.num_leaves) return;  // warp-uniform
+    const int K0 = KS ? KS : p.K0, K1 = KS ? KS : p.K1, K2 = KS ? KS : p.K2;
+    const int K = KS ? KS * KS * KS : p.K, Kp = K | 1;
+    uint8_t *base = kmap_smem + (size_t)warp * warp_bytes;
+    WinLeaf *win = reinterpret_cast<WinLeaf *>(base);
+    uint16_t *slots = reinterpret_cast<uint16_t *>(win + p.window);
+    int32_t *rows = reinterpret_cast<int32_t *>(slots + 512);
+    uint32_t *tmask = reinterpret_cast<uint32_t *>(rows + 32 * Kp);
+    int32_t *counts = reinterpret_cast<int32_t *>(tmask + 8);
+
+    const FvgbLeaf &tl = p.tgt.leaves[leaf_id];
+    const int32_t ox = tl.origin[0], oy = tl.origin[1], oz = tl.origin[2], b = tl.batch;
+    const int64_t tbase = tl.base;
+    // source footprint per ijk axis (axis 0 uses s2/k2, axis 2 s0/k0) and its leaf window
+    const int32_t lx0 = (ox * p.S2 + p.st2) >> 3, ly0 = (oy * p.S1 + p.st1) >> 3, lz0 = (oz * p.S0 + p.st0) >> 3;
+    const int32_t wx = (((ox + 7) * p.S2 + p.st2 + p.K2 - 1) >> 3) - lx0 + 1;
+    const int32_t wy = (((oy + 7) * p.S1 + p.st1 + p.K1 - 1) >> 3) - ly0 + 1;
+    const int32_t wz = (((oz + 7) * p.S0 + p.st0 + p.K0 - 1) >> 3) - lz0 + 1;
+    const int32_t W = wx * wy * wz;  // == p.window (the same for every leaf)
+
+    if (lane < 8) tmask[lane] = 0;
+    if (p.nbsizes)
+        for (int k = lane; k < K; k += 32) counts[k] = 0;
+    for (int w = lane; w < W; w += 32) {
+        const int32_t ix = w / (wy * wz), iy = (w / wz) % wy, iz = w % wz;
+        const int32_t id = find_leaf(p.src, b, lx0 + ix, ly0 + iy, lz0 + iz);
+        WinLeaf &dst = win[w];
+        if (id < 0) {
+            dst.base = -1;
+            continue;
+        }
+        const FvgbLeaf &sl = p.src.leaves[id];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) dst.mask[q] = sl.mask[q];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dst.prefix[q] = (uint32_t)sl.prefix[2 * q] | ((uint32_t)sl.prefix[2 * q + 1] << 16);
+        dst.base = sl.base;
+    }
+    {
+        // active slots in index (bit) order: lane covers slots [16*lane, 16*lane + 16)
+        const int word = lane >> 2, sh = (lane & 3) * 16;
+        const uint64_t m = tl.mask[word];
+        uint32_t bits16 = (uint32_t)(m >> sh) & 0xffffu;
+        uint32_t r = (uint32_t)tl.prefix[word] + (uint32_t)__popcll(m & ((1ull << sh) - 1ull));
+        while (bits16) {
+            const int bp = __ffs(bits16) - 1;
+            bits16 &= bits16 - 1;
+            slots[r++] = (uint16_t)(16 * lane + bp);
+        }
+    }
+    const int32_t cnt = (int32_t)tl.prefix[7] + __popcll(tl.mask[7]);
+    __syncwarp();
+
+    const int64_t t0 = tbase >> 7;  // first 128-row tile this leaf's rows touch
+    const int32_t bx0 = 8 * lx0 - p.st2, by0 = 8 * ly0 - p.st1, bz0 = 8 * lz0 - p.st0;
+    for (int32_t r0 = 0; r0 < cnt; r0 += 32) {
+        const int32_t r = r0 + lane;
+        if (r < cnt) {
+            const uint32_t s = slots[r];
+            // source coordinate of offset (0,0,0), relative to the window's first voxel (>= 0)
+            const int32_t ux = (ox + (int32_t)(s >> 6)) * p.S2 - bx0;
+            const int32_t uy = (oy + (int32_t)((s >> 3) & 7)) * p.S1 - by0;
+            const int32_t uz = (oz + (int32_t)(s & 7)) * p.S0 - bz0;
+            int32_t *dst = rows + lane * Kp;
+            uint32_t bits = 0;
+            int k = 0;
+#pragma unroll
+            for (int i2 = 0; i2 < K2; ++i2) {  // kIdx = (i2*K1 + i1)*K0 + i0
+                const int32_t vx = ux + i2;
+                const int32_t wxv = (vx >> 3) * wy;
+                const uint32_t bxv = (uint32_t)(vx & 7) << 6;
+#pragma unroll
+                for (int i1 = 0; i1 < K1; ++i1) {
+                    const int32_t vy = uy + i1;
+                    const int32_t wxy = (wxv + (vy >> 3)) * wz;
+                    const uint32_t bxy = bxv | ((uint32_t)(vy & 7) << 3);
+#pragma unroll
+                    for (int i0 = 0; i0 < K0; ++i0, ++k) {
+                        const int32_t vz = uz + i0;
+                        const WinLeaf &wl = win[wxy + (vz >> 3)];
+                        const uint32_t bit = bxy | (uint32_t)(vz & 7);
+                        const uint64_t m = wl.mask[bit >> 6];
+                        int32_t idx = -1;
+                        if (wl.base >= 0 && ((m >> (bit & 63)) & 1ull)) {
+                            idx = (int32_t)wl.base + (int32_t)win_prefix(wl, bit >> 6) +
+                                  __popcll(m & ((1ull << (bit & 63)) - 1ull));
+                            bits |= 1u << k;
+                            if (p.nbsizes) atomicAdd(&counts[k], 1);
+                        }
+                        dst[k] = idx;
+                    }
+                }
+            }
+            if (p.tile_mask && bits) atomicOr(&tmask[((tbase + r) >> 7) - t0], bits);
+        }
+        __syncwarp();
+        const int32_t nrows = min(32, cnt - r0);
+        if (p.ld == K && (KS > 0 || Kp == K)) {
+            int32_t *g = p.kmap + (tbase + r0) * K;  // the block of rows is contiguous in the map
+            for (int32_t e = lane; e < nrows * K; e += 32) {
+                const int32_t rr = e / K;  // a constant divisor when KS > 0
+                g[e] = rows[rr * Kp + (e - rr * K)];
+            }
+        } else {
+            for (int32_t rr = 0; rr < nrows; ++rr) {
+                int32_t *g = p.kmap + (tbase + r0 + rr) * p.ld;
+                for (int c = lane; c < K; c += 32) g[c] = rows[rr * Kp + c];
+            }
+        }
+        __syncwarp();
+    }
+    if (p.nbsizes)
+        for (int k = lane; k < K; k += 32)
+            if (counts[k]) atomicAdd(p.nbsizes + k, counts[k]);
+    if (p.tile_mask && lane < 8 && tmask[lane]) atomicOr(p.tile_mask + t0 + lane, tmask[lane]);
+}
+
 __global__ void fill_kernel(int32_t *__restrict__ p, int64_t n, int32_t v) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = v;
@@ -298,6 +434,22 @@ extern "C" int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const i
     p.window = W <= kMaxWindow ? (int32_t)W : 0;
     const int nk_smem = nbsizes ? (int)std::min<int64_t>(K, kMaxKSmem) : 0;
     p.disp_table = (K <= kMaxKSmem && ksize[0] <= 511 && ksize[1] <= 511 && ksize[2] <= 511) ? 1 : 0;
+    if (p.window > 0 && p.window <= kMaxWindowWarp && K <= 32) {
+        // one warp per target leaf (the common case: 3^3, 2^3, ... kernels)
+        const size_t wb = ((size_t)p.window * sizeof(WinLeaf) + 512 * sizeof(uint16_t) + 32 * (size_t)(K | 1) * 4 +
+                           8 * 4 + (nbsizes ? (size_t)K * 4 : 0) + 15) & ~(size_t)15;
+        const unsigned blocks = (unsigned)ceil_div(tgt->num_leaves, (int64_t)kWarpLeaves);
+        const size_t smem = wb * kWarpLeaves;
+        const bool cube = ksize[0] == ksize[1] && ksize[1] == ksize[2];
+        if (cube && ksize[0] == 3)
+            kmap_warp_kernel<3><<<blocks, 32 * kWarpLeaves, smem, as_stream(stream)>>>(p, (int32_t)wb);
+        else if (cube && ksize[0] == 2)
+            kmap_warp_kernel<2><<<blocks, 32 * kWarpLeaves, smem, as_stream(stream)>>>(p, (int32_t)wb);
+        else
+            kmap_warp_kernel<0><<<blocks, 32 * kWarpLeaves, smem, as_stream(stream)>>>(p, (int32_t)wb);
+        count_launches(1);
+        return launch_status();
+    }
     const size_t smem = (size_t)p.window * sizeof(WinLeaf) + 512 * sizeof(uint16_t) + nk_smem * 4 + 8 * 4 +
                         (p.disp_table ? (size_t)K * 4 : 0);
     kmap_leaf_kernel<<<(unsigned)tgt->num_leaves, kKmapThreads, smem, as_stream(stream)>>>(p);
