@@ -341,12 +341,10 @@ def run_gpu(args) -> None:
         x_host = x.cpu().pin_memory()
         e2e_steps = max(2, min(args.steps, 5))
         h2d = ijk_host.numel() * 4 + x_host.numel() * 2 + off_host.numel() * 8
-        torch.cuda.synchronize()
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        t0.record()
-        d2h = 0
-        for _ in range(e2e_steps):
+        out_host = None  # pinned result buffer, allocated once like a serving loop would
+
+        def e2e_step():
+            nonlocal out_host
             ijk_d = ijk_host.to(dev, non_blocking=True)
             x_d = x_host.to(dev, non_blocking=True)
             grid_e = fvdb.GridBatch.from_ijk(fvdb.JaggedTensor.from_data_and_offsets(ijk_d, off_host.to(dev, non_blocking=True)))
@@ -356,10 +354,23 @@ def run_gpu(args) -> None:
             x_sorted = torch.empty_like(x_d)
             x_sorted[idx] = x_d
             y_e, *_ = model.forward(grid_e, x_sorted)
-            out_host = y_e.to("cpu")
-            d2h = out_host.numel() * out_host.element_size()
-        t1.record()
+            if out_host is None or out_host.shape != y_e.shape:
+                out_host = torch.empty(y_e.shape, dtype=y_e.dtype).pin_memory()
+            out_host.copy_(y_e, non_blocking=True)
+            return out_host.numel() * out_host.element_size()
+
+        # warm-up: first calls of the end-to-end-only operations (large index_put, ijk_to_index)
+        for _ in range(max(args.warmup, 1)):
+            e2e_step()
         torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        d2h = 0
+        for _ in range(e2e_steps):
+            d2h = e2e_step()
+        t1.record()
+        torch.cuda.synchronize()  # the last result has reached host memory
         e2e_ms = t0.elapsed_time(t1) / e2e_steps
 
     kern_ms, kern_identical = kernel_only_l1(lib, p1, x, model.w1, max(args.steps, 3))

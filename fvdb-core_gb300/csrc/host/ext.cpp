@@ -137,6 +137,25 @@ GridPtr build_grid(const Tensor &ijk_in, const Tensor &joff_in, const Tensor &vs
     g->voxel_sizes = per_grid_vec(vs, B, "voxel_sizes");
     g->origins = per_grid_vec(org, B, "origins");
     auto i32 = torch::dtype(torch::kInt32).device(dev);
+    // Large inputs without known bounds: read their bounding box first (one small reduction and
+    // one read) so the radix sort covers only the order-key bits that vary (3 of 8 passes for
+    // coordinates in [0, 256)^3).  Small inputs sort the full key instead of paying the read.
+    int32_t mlo[3], mhi[3];
+    if (!(box_lo && box_hi) && n >= (int64_t)1 << 18) {
+        Tensor bx = torch::cat({std::get<0>(ijk.min(0)), std::get<0>(ijk.max(0))}).to(torch::kInt64);
+        int64_t *hb = pinned_meta(dev.index(), 6);
+        cudaStream_t cs = reinterpret_cast<cudaStream_t>(cur_stream());
+        TORCH_CHECK(cudaMemcpyAsync(hb, bx.data_ptr<int64_t>(), 6 * sizeof(int64_t), cudaMemcpyDeviceToHost, cs) ==
+                            cudaSuccess &&
+                        cudaStreamSynchronize(cs) == cudaSuccess,
+                    "grid build: reading the bounds failed");
+        for (int a = 0; a < 3; ++a) {
+            mlo[a] = (int32_t)hb[a];
+            mhi[a] = (int32_t)hb[3 + a];
+        }
+        box_lo = mlo;
+        box_hi = mhi;
+    }
     Tensor out_ijk = torch::empty({std::max<int64_t>(n, 1), 3}, i32);
     // device metadata read back in one copy: [0, B] voxel offsets, B+1 leaf count, B+2 voxel
     // count, B+3 error word (the sort's int32 flag in its low half; zero-initialised), then the

@@ -63,3 +63,23 @@ def test_coordinate_outside_box_is_reported(cuda_device):
     joff = torch.tensor([0, 3], dtype=torch.int64, device=cuda_device)
     assert _sort(lib, ijk, joff, ((0, 0, 0), (8, 8, 8)))[2] == FVGB_ERANGE
     assert _sort(lib, ijk, joff, ((0, 0, 0), (9, 8, 8)))[2] == 0
+
+
+def test_large_grid_build_sorts_within_measured_bounds(cuda_device):
+    """Inputs of >= 2^18 points are sorted over the key bits their measured bounding box allows;
+    the voxels and offsets equal the oracle's NanoVDB order (coordinates crossing zero and a
+    root-tile boundary)."""
+    import fvdb
+    from oracle import oracle as orc
+
+    rng = np.random.default_rng(11)
+    n = 300_000
+    ijk = np.stack([rng.integers(-700, 300, n), rng.integers(4000, 4400, n), rng.integers(-90, 90, n)],
+                   1).astype(np.int32)
+    off = np.array([0, 120_000, n], dtype=np.int64)
+    jt = fvdb.JaggedTensor.from_data_and_offsets(torch.from_numpy(ijk).to(cuda_device),
+                                                 torch.from_numpy(off).to(cuda_device))
+    grid = fvdb.GridBatch.from_ijk(jt)
+    ref, ref_off = orc.grid_from_ijk(ijk, off)
+    assert np.array_equal(grid.ijk.jdata.cpu().numpy(), ref)
+    assert np.array_equal(grid.joffsets.cpu().numpy(), ref_off)
