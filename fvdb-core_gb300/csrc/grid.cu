@@ -55,17 +55,22 @@ size_t sort_ws_layout(int64_t n, SortWs *ws, char *base) {
 
 // box_lo/box_hi: bounds every coordinate must lie in (the whole coordinate range when the
 // caller promises none); a coordinate outside raises FVGB_ERANGE.
+// fold > 0: every key agrees above bit `fold` (coordinates inside a box), so the grid index
+// replaces those bits and one radix sort orders by (grid, key).
 __global__ void keys_kernel(const int32_t *__restrict__ ijk, const int64_t *__restrict__ joff,
-                            int32_t B, int64_t n, int3 box_lo, int3 box_hi, uint64_t *__restrict__ keys,
-                            int32_t *__restrict__ bidx, int32_t *__restrict__ err) {
+                            int32_t B, int64_t n, int3 box_lo, int3 box_hi, int32_t fold,
+                            uint64_t *__restrict__ keys, int32_t *__restrict__ bidx, int32_t *__restrict__ err) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int32_t x = ijk[3 * i], y = ijk[3 * i + 1], z = ijk[3 * i + 2];
     if (!coord_in_range(x) || !coord_in_range(y) || !coord_in_range(z) || x < box_lo.x || x > box_hi.x ||
         y < box_lo.y || y > box_hi.y || z < box_lo.z || z > box_hi.z)
         atomicExch(err, FVGB_ERANGE);
-    keys[i] = order_key(x, y, z);
-    bidx[i] = batch_of(joff, B, i);
+    const int32_t b = batch_of(joff, B, i);
+    uint64_t k = order_key(x, y, z);
+    if (fold > 0) k = (k & ((1ull << fold) - 1ull)) | ((uint64_t)b << fold);
+    keys[i] = k;
+    bidx[i] = b;
 }
 
 // One past the highest order_key bit that can differ between coordinates in [lo, hi] (per
@@ -109,16 +114,18 @@ __global__ void unique_flags_kernel(const uint64_t *__restrict__ keys,
     flags[i] = (i == 0 || keys[i] != keys[i - 1] || bidx[i] != bidx[i - 1]) ? 1 : 0;
 }
 
+// low_mask / high: a folded key keeps the order key's bits under low_mask; the bits above are
+// `high` for every voxel (no folding: low_mask all ones, high zero).
 __global__ void unique_write_kernel(const uint64_t *__restrict__ keys,
                                     const int32_t *__restrict__ bidx,
-                                    const int32_t *__restrict__ pos, int64_t n,
-                                    int32_t *__restrict__ out_ijk) {
+                                    const int32_t *__restrict__ pos, int64_t n, uint64_t low_mask,
+                                    uint64_t high, int32_t *__restrict__ out_ijk) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const bool first = (i == 0 || keys[i] != keys[i - 1] || bidx[i] != bidx[i - 1]);
     if (!first) return;
     int32_t x, y, z;
-    key_to_coord(keys[i], x, y, z);
+    key_to_coord((keys[i] & low_mask) | high, x, y, z);
     const int64_t p = pos[i];
     out_ijk[3 * p] = x;
     out_ijk[3 * p + 1] = y;
@@ -317,18 +324,28 @@ int sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids, 
         hi = make_int3(box_hi[0], box_hi[1], box_hi[2]);
         end_bit = order_key_end_bit(box_lo, box_hi);
     }
-    keys_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, joffsets, num_grids, n, lo, hi, w.keys_a, w.bidx_a, err_dev);
+    int grid_bits = 0;
+    while ((1ll << grid_bits) < num_grids) ++grid_bits;
+    // inside a box the keys agree above end_bit: the grid index takes those bits (one sort)
+    const int fold = (box_lo && box_hi && num_grids > 1 && end_bit + grid_bits <= 63) ? end_bit : 0;
+    uint64_t low_mask = ~0ull, high = 0;
+    if (fold) {
+        low_mask = (1ull << fold) - 1ull;
+        high = order_key(box_lo[0], box_lo[1], box_lo[2]) & ~low_mask;
+    }
+    keys_kernel<<<blocks_for(n), kThreads, 0, s>>>(ijk, joffsets, num_grids, n, lo, hi, fold, w.keys_a, w.bidx_a,
+                                                   err_dev);
     size_t tb = w.cub_bytes;
     // 1) sort by voxel key (stable radix, only the bits that can differ), 2) stable sort by grid
-    //    index: grids stay contiguous and every grid's voxels stay in key order.
-    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.bidx_a, w.bidx_b, n, 0, end_bit, s);
+    //    index -- or one sort when the grid index is folded into the key: grids stay contiguous
+    //    and every grid's voxels stay in key order.
+    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.bidx_a, w.bidx_b, n, 0,
+                                    fold ? fold + grid_bits : end_bit, s);
     const uint64_t *keys = w.keys_b;
     const int32_t *bidx = w.bidx_b;
-    if (num_grids > 1) {
-        int bits = 1;
-        while ((1ll << bits) < num_grids) ++bits;
+    if (num_grids > 1 && !fold) {
         tb = w.cub_bytes;
-        cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.bidx_b, w.bidx_a, w.keys_b, w.keys_a, n, 0, bits, s);
+        cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.bidx_b, w.bidx_a, w.keys_b, w.keys_a, n, 0, grid_bits, s);
         keys = w.keys_a;
         bidx = w.bidx_a;
     }
@@ -337,7 +354,7 @@ int sort_unique(const int32_t *ijk, const int64_t *joffsets, int32_t num_grids, 
     // exclusive scan in place over n+1 flags: pos[n] = unique count
     int32_t *pos = reinterpret_cast<int32_t *>(w.keys_a == keys ? (void *)w.keys_b : (void *)w.keys_a);
     cub::DeviceScan::ExclusiveSum(w.cub_tmp, tb, w.flags, pos, n + 1, s);
-    unique_write_kernel<<<blocks_for(n), kThreads, 0, s>>>(keys, bidx, pos, n, out_ijk);
+    unique_write_kernel<<<blocks_for(n), kThreads, 0, s>>>(keys, bidx, pos, n, low_mask, high, out_ijk);
     offsets_kernel<<<(unsigned)ceil_div(num_grids + 1, kThreads), kThreads, 0, s>>>(bidx, pos, n, num_grids,
                                                                                     out_joffsets);
     count_launches(4);
