@@ -359,3 +359,32 @@ extern "C" int fvgb_conv_wgrad_tc(const void *x, int64_t n_x, int32_t c_in, int6
     count_launches(launched + 1);
     return launch_status();
 }
+
+namespace fvgb {
+namespace {
+// One CTA: thread 0 waits on an mbarrier phase with the same bounded wait the tensor-core
+// kernels use.  Without `arrive` nothing completes the phase, so the wait must give up after
+// `budget` cycles and report FVGB_ETIMEOUT; with `arrive` the phase is already complete.
+__global__ void selftest_wait_kernel(int32_t *err, long long budget, int32_t arrive) {
+    __shared__ uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        abort_flag = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (arrive) tc::mbar_arrive(&bar);
+        if (!tc::mbar_wait_budget(&bar, 0, &abort_flag, budget)) atomicExch(err, FVGB_ETIMEOUT);
+    }
+}
+}  // namespace
+}  // namespace fvgb
+
+extern "C" int fvgb_selftest_wait_timeout(int32_t *err_dev, int64_t budget_cycles, int32_t arrive,
+                                          fvgb_stream_t stream) {
+    if (!err_dev || budget_cycles < 1 || budget_cycles > ((int64_t)1 << 32)) return FVGB_EINVAL;
+    fvgb::selftest_wait_kernel<<<1, 32, 0, fvgb::as_stream(stream)>>>(err_dev, (long long)budget_cycles, arrive);
+    fvgb::count_launches(1);
+    return fvgb::launch_status();
+}

@@ -51,18 +51,24 @@ constexpr long long kWaitCycles = 1ll << 31;
 constexpr uint32_t kSuspendNs = 1000000;
 
 // Waits for the phase of `parity` to complete.  Returns false (and raises *abort) if it did
-// not within kWaitCycles or if another thread of the CTA already aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
+// not within `budget` SM cycles or if another thread of the CTA already aborted.
+__device__ __forceinline__ bool mbar_wait_budget(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                                 long long budget) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
         if (mbar_try_wait_sleep(bar, parity, kSuspendNs)) return true;
         if (*abort) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > budget) {
             *abort = 1;
             return false;
         }
     }
+}
+
+// mbar_wait_budget with the kernels' budget, kWaitCycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
+    return mbar_wait_budget(bar, parity, abort, kWaitCycles);
 }
 
 // mbar_wait for waits off the critical path (a warp idle for a whole tile): between polls the

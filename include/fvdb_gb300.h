@@ -333,6 +333,18 @@ int fvgb_conv_wgrad_tc(const void *x, int64_t n_x, int32_t c_in, int64_t ldx, co
 int fvgb_quantize_e4m3(int32_t dtype, const void *x, int64_t n, int32_t c, int64_t ldx, const float *inv_scale,
                        void *out, int64_t ldo, fvgb_stream_t stream);
 
+/* ------------------------------------------------------------------- self test --- */
+
+/*
+ * Exercises the bounded wait every tensor-core kernel uses (about one second there): one
+ * thread waits on an mbarrier phase for at most budget_cycles SM cycles (1..2^32).  With
+ * arrive == 0 nothing completes the phase, so the wait gives up and *err_dev (caller-zeroed
+ * device int32) becomes FVGB_ETIMEOUT; with arrive != 0 the phase completes first and *err_dev
+ * stays 0.  The GPU context stays usable either way.  No counterpart in the reference (its
+ * kernels have no in-kernel waits).
+ */
+int fvgb_selftest_wait_timeout(int32_t *err_dev, int64_t budget_cycles, int32_t arrive, fvgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,3 +38,11 @@ def test_host_only_entry_points():
     # argument validation happens before any device work
     assert lib.fvgb_ijk_sort_unique_workspace(ctypes.c_int64(-1), ctypes.c_int32(1), ctypes.byref(n)) == 1
     assert lib.fvgb_kmap_masks(None, ctypes.c_int64(10), ctypes.c_int32(40), ctypes.c_int64(40), None, None, None) == 1
+
+
+def test_selftest_wait_rejects_bad_arguments_without_a_gpu():
+    """Argument checks of fvgb_selftest_wait_timeout return FVGB_EINVAL before any device work."""
+    lib = ctypes.CDLL(LIB)
+    assert lib.fvgb_selftest_wait_timeout(None, ctypes.c_int64(100), 0, None) == 1
+    assert lib.fvgb_selftest_wait_timeout(ctypes.c_void_p(16), ctypes.c_int64(0), 0, None) == 1
+    assert lib.fvgb_selftest_wait_timeout(ctypes.c_void_p(16), ctypes.c_int64(1 << 40), 0, None) == 1
