@@ -10,7 +10,9 @@ namespace {
 using namespace tc;
 
 constexpr int kTileM = 128;
-constexpr int kThreads = 160;
+constexpr int kWgGatherWarps = 8;  // 256 gather threads: cp.async throughput grows with the issuing warps
+constexpr int kWgMmaWarp = kWgGatherWarps;
+constexpr int kThreads = (kWgGatherWarps + 1) * 32;
 
 }  // namespace
 }  // namespace fvgb
@@ -79,7 +81,11 @@ extern "C" int fvgb_quantize_e4m3(int32_t dtype, const void *x, int64_t n, int32
 namespace fvgb {
 namespace {
 
-constexpr int kMNAtom = 16384;  // 128 K-rows x 128 bytes: one 64-element-wide MN atom of a stage
+constexpr int kMNAtom = 16384;
+
+__device__ __forceinline__ void st_shared_zero16(uint32_t addr) {
+    asm volatile("st.shared.v4.u32 [%0], {%1, %1, %1, %1};" ::"r"(addr), "r"(0) : "memory");
+}  // 128 K-rows x 128 bytes: one 64-element-wide MN atom of a stage
 
 // MN-major operand, 128B swizzle: MN atoms (64 elements) kMNAtom apart (LBO), 8-row K groups
 // 1024 bytes apart (SBO).
@@ -142,13 +148,13 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&full[s], kTileM / 32);  // one arrival per gather warp
+            mbar_init(&full[s], kWgGatherWarps);  // one arrival per gather warp
             mbar_init(&empty[s], 1);
         }
         mbar_init(accum, 1);
         *abort = 0;
     }
-    if (warp == 4) tmem_alloc(tmem_slot, BN);
+    if (warp == kWgMmaWarp) tmem_alloc(tmem_slot, BN);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -161,52 +167,109 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
     };
 
     int steps = 0;  // active stages: the gather warps run the same loop as the MMA thread
-    if (warp < 4) {
-        const int r = threadIdx.x;
-        int it = 0, sig = 0;
+    if (warp < kWgGatherWarps) {
+        // Lane -> (16-byte chunk jj of a 128-byte MN atom row, K-rows rsub + 4q of this warp's
+        // 16): one warp instruction moves four whole 128-byte atom rows of an operand.  Atom a of
+        // the A operand holds M elements a*64 .. a*64+63, i.e. offset (a*64 + 8*jj) / cin of the
+        // group at channel (a*64 + 8*jj) % cin.
+        const int jj = lane & 7, rsub = lane >> 3, row0 = warp * (kTileM / kWgGatherWarps);
+        int joff[2], ci0[2];
+#pragma unroll
+        for (int at = 0; at < 2; ++at) {
+            const int m0 = at * 64 + jj * 8;
+            joff[at] = m0 / a.cin;
+            ci0[at] = m0 - joff[at] * a.cin;
+        }
+        uint32_t it = 0, sig = 0, stage = 0, phase = 0, pstage = 0;
         for (int64_t t = 0; t < n_tiles; ++t)
             if (tile_active(t)) ++steps;
-        for (int64_t t = 0; t < n_tiles && !*abort; ++t) {
-            if (!tile_active(t)) continue;
-            const int stage = it % S;
-            if (!__all_sync(0xffffffffu, mbar_wait(&empty[stage], ((it / S) & 1) ^ 1, abort))) break;
-            const uint32_t base = smem_u32(smem + stage * kStage);
-            const int64_t m = r_begin + t * kTileM + r;
-            const bool row_ok = m < r_end;
-            // B: dy row m, c_out channels
-            const uint8_t *dyrow = a.dy + (row_ok ? m : 0) * a.lddy_bytes;
-            for (int e = 0; e < a.cout; e += 8)
-                cp_async_16(base + kBOff + mn_offset(r, e), dyrow + e * 2, row_ok ? 16u : 0u);
-            // A: the G gathered feature rows, stacked along M
-            for (int j = 0; j < G; ++j) {
-                int32_t src = -1;
-                if (row_ok && j < ng) {
-                    src = a.map[m * a.K + k0 + j];
-                    if (src >= a.n_x) src = -1;
+        // map entries of a tile for this lane's rows; loaded one active tile ahead, so their
+        // latency overlaps the previous stage's copies instead of stalling the next
+        auto load_src = [&](int64_t t, int32_t (&dst)[2][4]) {
+#pragma unroll
+            for (int at = 0; at < 2; ++at)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int64_t m = r_begin + t * kTileM + row0 + rsub + 4 * q;
+                    int32_t v = -1;
+                    if (m < r_end && joff[at] < ng) {
+                        v = a.map[m * a.K + k0 + joff[at]];
+                        if (v >= a.n_x) v = -1;
+                    }
+                    dst[at][q] = v;
                 }
-                const uint8_t *xrow = a.x + (src >= 0 ? (int64_t)src * a.ldx_bytes : 0);
-                for (int e = 0; e < a.cin; e += 8)
-                    cp_async_16(base + mn_offset(r, j * a.cin + e), xrow + e * 2, src >= 0 ? 16u : 0u);
+        };
+        auto next_active = [&](int64_t t) {
+            while (t < n_tiles && !tile_active(t)) ++t;
+            return t;
+        };
+        int32_t src_next[2][4];
+        int64_t t = next_active(0);
+        if (t < n_tiles) load_src(t, src_next);
+        for (; t < n_tiles && !*abort;) {
+            int32_t src[2][4];
+#pragma unroll
+            for (int at = 0; at < 2; ++at)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) src[at][q] = src_next[at][q];
+            const int64_t t_next = next_active(t + 1);
+            if (t_next < n_tiles) load_src(t_next, src_next);
+            bool go = true;
+            if (lane == 0) go = mbar_wait(&empty[stage], phase ^ 1, abort);
+            go = __shfl_sync(0xffffffffu, go, 0);
+            __syncwarp();
+            if (!go) break;
+            const uint32_t base = smem_u32(smem + stage * kStage);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int r = row0 + rsub + 4 * q;
+                const int64_t m = r_begin + t * kTileM + r;
+                // B: dy row m, all c_out channels (BN/64 atoms)
+#pragma unroll
+                for (int at = 0; at < BN / 64; ++at) {
+                    const uint32_t dst = base + kBOff + mn_offset(r, at * 64 + jj * 8);
+                    if (m < r_end)
+                        cp_async_16(dst, a.dy + m * a.lddy_bytes + at * 128 + jj * 16, 16u);
+                    else
+                        st_shared_zero16(dst);
+                }
+                // A: the group's gathered feature rows, stacked along M
+#pragma unroll
+                for (int at = 0; at < 2; ++at) {
+                    const uint32_t dst = base + mn_offset(r, at * 64 + jj * 8);
+                    if (src[at][q] >= 0)
+                        cp_async_16(dst, a.x + (int64_t)src[at][q] * a.ldx_bytes + ci0[at] * 2, 16u);
+                    else
+                        st_shared_zero16(dst);
+                }
             }
-            // cp.async writes are generic-proxy writes: each thread fences its own copies to the
-            // tensor core (async proxy), one step late, so the MMA thread never fences; one lane
-            // per warp then arrives (per-thread arrivals on one barrier word serialise)
+            // cp.async and st.shared are generic-proxy writes: each warp fences its own copies to
+            // the tensor core (async proxy), one stage late, so the MMA thread never fences
             cp_async_commit();
             ++it;
+            if (++stage == (uint32_t)S) {
+                stage = 0;
+                phase ^= 1;
+            }
             if (it - sig > 1) {
                 cp_async_wait_group<1>();
                 fence_proxy_async();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&full[sig % S]);
+                if (lane == 0) mbar_arrive(&full[pstage]);
                 ++sig;
+                if (++pstage == (uint32_t)S) pstage = 0;
             }
+            t = t_next;
         }
         cp_async_wait_group<0>();
         fence_proxy_async();
         __syncwarp();
         if (lane == 0)
-            for (; sig < it; ++sig) mbar_arrive(&full[sig % S]);
-    } else if (warp == 4 && lane == 0) {
+            for (; sig < it; ++sig) {
+                mbar_arrive(&full[pstage]);
+                if (++pstage == (uint32_t)S) pstage = 0;
+            }
+    } else if (warp == kWgMmaWarp && lane == 0) {
         constexpr uint32_t idesc = idesc_m128(BN, 1, 1) | (1u << 15) | (1u << 16);  // bf16, A and B MN-major
         int it = 0;
         for (int64_t t = 0; t < n_tiles; ++t) {
@@ -253,7 +316,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4) {
+    if (warp == kWgMmaWarp) {
         tc_fence_after();
         tmem_dealloc(tmem, BN);
     }
