@@ -544,6 +544,17 @@ def leg_train(fvdb, dev, args) -> dict:
     res["bf16"]["errors_vs_fp64_same_rounding"] = {
         "y": rel_errors(outs["bf16"][0], bf(y2.detach())), "dx": rel_errors(outs["bf16"][1], bf(dxq)),
         "dw1": rel_errors(outs["bf16"][2], bf(dw1q))}
+    # One SparseConv3d (3^3, 64->64) forward + backward, BF16 vs FP64 on the unrounded inputs:
+    # without a ReLU between layers no mask can flip, so this is the layer's own BF16 error.
+    one = {}
+    for name, dtype in (("bf16", torch.bfloat16), ("fp64", torch.float64)):
+        xs = x0.to(dev, dtype).requires_grad_(True)
+        ws = w1.to(dev, dtype).requires_grad_(True)
+        ys = pack.sparse_conv_3d(xs, ws).jdata
+        ys.backward(dy.to(dev, dtype))
+        one[name] = (ys.detach(), xs.grad.detach(), ws.grad.detach())
+    res["bf16"]["single_layer_errors_vs_fp64"] = {
+        k: rel_errors(o, r) for k, o, r in zip(("y", "dx", "dw"), one["bf16"], one["fp64"])}
     return res
 
 

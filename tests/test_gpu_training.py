@@ -190,3 +190,30 @@ def test_recompute_matches_and_saves_memory(cuda_device):
     assert torch.allclose(grads[0][0], grads[1][0], rtol=1e-2, atol=1e-2)
     assert torch.allclose(grads[0][1], grads[1][1], rtol=1e-2, atol=1e-2)
     assert held[1] < held[0]
+
+
+def test_single_layer_bf16_forward_backward_within_1e2_of_fp64(cuda_device):
+    """One SparseConv3d (3^3, 64->64) in BF16 -- forward, data gradient and weight gradient on
+    tcgen05 -- against FP64 on the unrounded inputs: rel-L2 <= 1e-2 for y, dx and dW (the BF16
+    rounding of inputs, weights and outputs is the whole error; no ReLU mask can flip)."""
+    import fvdb
+
+    from tests.synth import box_surfaces
+
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(box_surfaces(8, 96, 300)).to(cuda_device))
+    pack, _ = grid.sparse_conv_kernel_map(3, 1)
+    g = torch.Generator().manual_seed(301)
+    x0 = torch.randn(grid.total_voxels, 64, generator=g, dtype=torch.float64)
+    w0 = torch.randn(64, 64, 3, 3, 3, generator=g, dtype=torch.float64) * math.sqrt(2.0 / (27 * 64))
+    dy = torch.randn(grid.total_voxels, 64, generator=g, dtype=torch.float64)
+    res = {}
+    for dtype in (torch.bfloat16, torch.float64):
+        x = x0.to(cuda_device, dtype).requires_grad_(True)
+        w = w0.to(cuda_device, dtype).requires_grad_(True)
+        y = pack.sparse_conv_3d(x, w).jdata
+        y.backward(dy.to(cuda_device, dtype))
+        res[dtype] = (y.detach().double().cpu().numpy(), x.grad.double().cpu().numpy(), w.grad.double().cpu().numpy())
+    torch.cuda.synchronize()
+    fvdb._lib.load().check_device_errors(cuda_device)
+    for got, ref in zip(res[torch.bfloat16], res[torch.float64]):
+        assert rel_l2(got, ref) <= 1e-2
