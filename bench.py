@@ -422,6 +422,7 @@ def run_gpu(args) -> None:
                                 "sample": f"layer 1 (3^3 32->64) of grid 0 restricted to {r['voxels']} voxels, fp32, kernel map + gather/torch.mm/scatter ({r['seconds']:.2f} s)"}
     if not args.no_extras:
         line["fp32_plain"] = leg_fp32(fvdb, grid, x, model, flops, args)
+        line["c1_fp32"] = leg_c1(fvdb, dev, args)
         line["bf16_vs_fp32"] = tf / line["fp32_plain"]["value"] if line["fp32_plain"]["value"] else None
         line["train_c3"] = leg_train(fvdb, dev, args)
         line["fp8_c4"] = leg_fp8(fvdb, dev, args)
@@ -464,7 +465,39 @@ def leg_fp32(fvdb, grid, x, model, flops, args) -> dict:
         p2.sparse_conv_3d(h, w2)
 
     ms = time_ms(step, max(2, args.steps // 2), 1)
-    return {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms, "dtype": "f32"}
+    # errors of the BF16 step (the headline) and of this FP32 form against the same step in FP64
+    y16, *_ = model.forward(grid, x)
+    p1, _ = grid.sparse_conv_kernel_map(3, 1)
+    p2, _ = grid.sparse_conv_kernel_map(2, 2)
+    y64 = p2.sparse_conv_3d(p1.sparse_conv_3d(x.double(), model.w1.double()).jdata, model.w2.double()).jdata
+    y32 = p2.sparse_conv_3d(p1.sparse_conv_3d(xf, w1).jdata, w2).jdata
+    return {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms, "dtype": "f32",
+            "errors_vs_fp64": {"bf16_step": rel_errors(y16, y64), "fp32_step": rel_errors(y32, y64)}}
+
+
+def leg_c1(fvdb, dev, args) -> dict:
+    """C1, the reference's CPU-sized case: 20,000 voxels drawn from 64^3 (seed 0), 16 -> 16
+    channels, 3^3, FP32, no bias.  Forward time (kernel map included) and errors vs FP64."""
+    g = torch.Generator().manual_seed(0)
+    idx = torch.randperm(64 ** 3, generator=g)[:20000]
+    ijk = torch.stack([idx // 4096, idx // 64 % 64, idx % 64], 1).to(dev, torch.int32)
+    grid = fvdb.GridBatch.from_ijk(ijk)
+    x = torch.randn(grid.total_voxels, 16, generator=g)
+    w = torch.randn(16, 16, 3, 3, 3, generator=g) * math.sqrt(1.0 / (27 * 16))
+    xf, wf = x.to(dev), w.to(dev)
+
+    def step():
+        p, _ = grid.sparse_conv_kernel_map(3, 1)
+        return p.sparse_conv_3d(xf, wf).jdata
+
+    ms = time_ms(step, max(3, args.steps), 2)
+    y32 = step()
+    p, _ = grid.sparse_conv_kernel_map(3, 1)
+    y64 = p.sparse_conv_3d(x.double().to(dev), w.double().to(dev)).jdata
+    P = int((p.out_in_map >= 0).sum())
+    return {"voxels": grid.total_voxels, "pairs": P, "ms_per_step": ms, "us_per_step": ms * 1e3,
+            "voxels_per_s": grid.total_voxels / (ms * 1e-3), "useful_tflops": 2.0 * P * 16 * 16 / (ms * 1e-3) / 1e12,
+            "dtype": "f32", "errors_vs_fp64": rel_errors(y32, y64)}
 
 
 def box_surface_ijk(n_boxes: int, resolution: int, seed: int, device) -> torch.Tensor:
