@@ -13,14 +13,14 @@
 // kernel, and tcgen05.mma with N <= 128 costs the same ~60-80 cycles whatever N is.
 //
 // Warp roles (448 threads):
-//   warps 0-7  gather: each warp fills 16 rows of the A tile.  Lane l copies 16-byte chunk l%8 of
+//   warps 0-7  gather: each warp fills 16 rows of every unit's A tile.  Lane l copies chunk l%8 of
 //              rows l/8, l/8+4, l/8+8, l/8+12, so one warp instruction moves four whole 128-byte
 //              A rows (per-SM cp.async throughput is set by the number of issuing warps and the
 //              distinct lines per instruction, not by bytes).  Copies are 16-byte cp.async (L2
 //              evict_last: the input features stay L2-resident while the map and output stream)
 //              into the 128B-swizzled K-major A layout; absent entries (map -1) are zero-stored
 //              with st.shared.  Both are generic-proxy writes, so each warp publishes a stage to
-//              the tensor core (async proxy) itself, kLag steps late: cp.async.wait_group,
+//              the tensor core (async proxy) itself, kLag stages late: cp.async.wait_group,
 //              fence.proxy.async, __syncwarp, one mbarrier arrive.  The MMA thread never fences
 //              and its MMAs stream back to back.  Map entries are read before the stage wait so
 //              their latency overlaps it.
