@@ -69,6 +69,7 @@ def _per_grid(v, n: int) -> torch.Tensor:
 class GridBatch:
     def __init__(self, *, impl):
         self._impl = impl
+        self._halo_pack = None  # stride-1 3^3 kernel map for sparse_conv_halo, built on first use
 
     # ---------------------------------------------------------------- constructors -------
     @classmethod
@@ -142,6 +143,41 @@ class GridBatch:
         C = _lib.load()
         impl = C.PackInfoImpl(ks, st, self._impl, tgt)
         return SparseConvPackInfo(impl=impl), GridBatch(impl=impl.target_grid)
+
+    def sparse_conv_halo(self, input: JaggedTensor, weight: torch.Tensor, variant: int = 8) -> JaggedTensor:
+        """Stride-1 3x3x3 convolution of `input` (one feature row per voxel) over this grid, with
+        the reference's arguments, checks and error types (GridBatch.cpp:776-793,
+        autograd/SparseConvolutionHalo.cpp:17-86).  The reference computes it from a 10^3 halo
+        per leaf whose x, y, z offsets meet weight dims 4, 3, 2 (K2, K1, K0): the kernel map's
+        convention, so the result is sparse_conv_3d over the grid's stride-1 3^3 map, with the
+        same data and weight gradients.  `variant` picks one of the reference's halo kernels and
+        is accepted for compatibility (there is one implementation)."""
+        if not isinstance(input, JaggedTensor):
+            raise TypeError("input must be a JaggedTensor")
+        data = input.jdata
+        if not data.is_floating_point():
+            raise TypeError("input must have a floating point type")
+        if data.shape[0] != self.total_voxels:
+            raise ValueError("Value count not match!")
+        if input.num_outer_lists() != self.grid_count:
+            raise ValueError("Batch size not match!")
+        if not weight.is_floating_point():
+            raise TypeError("kernels must have a floating point type")
+        if weight.dim() != 5:
+            raise ValueError(
+                f"Expected kernels to have 5 dimensions (shape (out_ch, in_ch, d, h, w)) but got {weight.dim()} dimensions")
+        if not (weight.shape[2] == weight.shape[3] == weight.shape[4] == 3):
+            raise NotImplementedError("sparse_conv_halo only supports kernels of size 3x3x3")
+        if not data.is_contiguous():
+            raise ValueError("features must be contiguous")
+        if data.dim() != 2:
+            raise ValueError(f"Expected features to have 2 dimensions (shape (n, nF)) but got {data.dim()} dimensions")
+        if weight.shape[1] != data.shape[1]:
+            raise ValueError(f"Expected input channels of kernels ({weight.shape[1]}) to equal input channels of "
+                             f"features: {data.shape[1]}")
+        if self._halo_pack is None:
+            self._halo_pack, _ = self.sparse_conv_kernel_map(3, 1)
+        return input.jagged_like(self._halo_pack.sparse_conv_3d(data, weight).jdata)
 
     # ---------------------------------------------------------------- properties --------
     @property
