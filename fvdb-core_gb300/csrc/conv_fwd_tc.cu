@@ -82,6 +82,7 @@ struct FwdArgs {
     uint8_t *y;                 // bf16 [n_out, ldy]
     int64_t ldy;
     const float *scale;         // per output channel, may be null
+    const float *bias;          // per output channel, added after the scale, may be null
     int32_t *err;
     int32_t stages;
     int64_t n_tiles;
@@ -404,6 +405,10 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                         lo *= cc < a.cout ? a.scale[cc] : 0.f;
                         hi *= cc + 1 < a.cout ? a.scale[cc + 1] : 0.f;
                     }
+                    if (a.bias) {
+                        lo += cc < a.cout ? a.bias[cc] : 0.f;
+                        hi += cc + 1 < a.cout ? a.bias[cc + 1] : 0.f;
+                    }
                     __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
                     packed[t] = *reinterpret_cast<uint32_t *>(&h);
                 }
@@ -641,6 +646,15 @@ extern "C" int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32
                                 const int32_t *map, int64_t n_out, int32_t K, const uint32_t *tile_mask,
                                 const void *packed_w, int32_t c_out, void *y, int64_t ldy, const float *out_scale,
                                 int32_t *err_dev, fvgb_stream_t stream) {
+    return fvgb_conv_fwd_tc_bias(dtype, x, n_x, c_in, ldx, map, n_out, K, tile_mask, packed_w, c_out, y, ldy,
+                                 out_scale, nullptr, err_dev, stream);
+}
+
+extern "C" int fvgb_conv_fwd_tc_bias(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                     const int32_t *map, int64_t n_out, int32_t K, const uint32_t *tile_mask,
+                                     const void *packed_w, int32_t c_out, void *y, int64_t ldy,
+                                     const float *out_scale, const float *bias, int32_t *err_dev,
+                                     fvgb_stream_t stream) {
     const int eb = dtype == FVGB_E4M3 ? 1 : (dtype == FVGB_BF16 ? 2 : 0);
     if (!eb) return FVGB_ETYPE;
     if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldx < c_in || ldy < c_out || !err_dev)
@@ -677,6 +691,7 @@ extern "C" int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32
     a.y = (uint8_t *)y;
     a.ldy = ldy;
     a.scale = out_scale;
+    a.bias = bias;
     a.err = err_dev;
     a.stages = 0;
     a.n_tiles = ceil_div(n_out, kTileM);

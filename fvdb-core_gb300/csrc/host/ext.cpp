@@ -559,8 +559,10 @@ bool use_tensor_cores(const Tensor &x, int64_t cin, int64_t cout) {
 }
 
 // y[m] = sum_k x[map[m,k]] W[k]   for the first n_out rows of map
+// bias (optional, [cout]): added in the tensor-core epilogue, else after the contraction.
 Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &Wkio, bool transpose_w,
-                   const std::optional<Tensor> &tile_mask = std::nullopt) {
+                   const std::optional<Tensor> &tile_mask = std::nullopt,
+                   const std::optional<Tensor> &bias = std::nullopt) {
     c10::cuda::CUDAGuard guard(x.device());
     const int64_t K = map.size(1);
     const int64_t cin = transpose_w ? Wkio.size(2) : Wkio.size(1);
@@ -580,11 +582,15 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
                                           packed.data_ptr(), wb, s),
                      "weight pack");
         const uint32_t *tm = tile_mask ? reinterpret_cast<const uint32_t *>(tile_mask->data_ptr<int32_t>()) : nullptr;
-        check_status(fvgb_conv_fwd_tc(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
-                                      map.data_ptr<int32_t>(), n_out, (int32_t)K, tm, packed.data_ptr(), (int32_t)cout,
-                                      y.data_ptr(), y.stride(0), nullptr,
-                                      device_error_flag(x.device()).data_ptr<int32_t>(), s),
+        Tensor b32;
+        if (bias) b32 = bias->to(torch::kFloat32).contiguous();
+        check_status(fvgb_conv_fwd_tc_bias(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
+                                           map.data_ptr<int32_t>(), n_out, (int32_t)K, tm, packed.data_ptr(),
+                                           (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
+                                           bias ? b32.data_ptr<float>() : nullptr,
+                                           device_error_flag(x.device()).data_ptr<int32_t>(), s),
                      "sparse conv forward (tensor cores)");
+        return y;
     } else if (dt == FVGB_F32 || dt == FVGB_F64) {
         check_status(fvgb_conv_fwd_simt(dt, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0), map.data_ptr<int32_t>(),
                                         n_out, (int32_t)K, map.stride(0), w.data_ptr(), wsk, wsci, wsco, y.data_ptr(),
@@ -603,6 +609,7 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
                      "sparse conv forward");
         y.copy_(yf);
     }
+    if (bias) y.add_(bias->to(y.scalar_type()));
     return y;
 }
 
@@ -645,7 +652,8 @@ Tensor gather_wgrad(const Tensor &x, const Tensor &map, int64_t n_out, const Ten
 // ------------------------------------------------------------------------------------------
 // Forward / backward of one sparse convolution, called by the Python autograd Function.
 // Checks and permutes follow SparseConvolutionKernelMap.cpp:18-191.
-std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed) {
+std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed,
+                                 const std::optional<Tensor> &bias = std::nullopt) {
     TORCH_CHECK_VALUE(x.is_contiguous(), "features must be contiguous");
     TORCH_CHECK_TYPE(x.is_floating_point(), "features must have a floating point type");
     TORCH_CHECK_VALUE(x.dim() == 2, "Expected features to have 2 dimensions (shape (n, nF)) but got ", x.dim(),
@@ -677,12 +685,16 @@ std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr
         cout = weights.size(1);
         Wkio = weights.permute({4, 3, 2, 0, 1}).reshape({-1, cin, cout});
     }
+    if (bias) {
+        TORCH_CHECK_VALUE(bias->dim() == 1 && bias->size(0) == cout, "bias must have shape (", cout, ",)");
+        TORCH_CHECK_VALUE(bias->device() == x.device(), "bias must be on the features' device");
+    }
     Tensor y;
     if (!transposed)
-        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false))
+        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false), bias)
                       : torch::empty({0, cout}, x.options());
     else
-        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true))
+        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true), bias)
                       : torch::empty({0, cout}, x.options());
     return {y, Wkio};
 }
@@ -819,7 +831,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def_property_readonly("use_me", [](const PackInfo &p) { return p.use_me; })
         .def_property_readonly("use_tf32", [](const PackInfo &p) { return p.use_tf32; });
 
-    m.def("conv_forward", &conv_forward);
+    m.def("conv_forward", &conv_forward, py::arg("features"), py::arg("weights"), py::arg("pack"),
+          py::arg("transposed"), py::arg("bias") = py::none());
     m.def("conv_forward_fp8", &conv_forward_fp8);
     m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); });
     m.def("conv_backward", &conv_backward);

@@ -17,24 +17,30 @@ from . import _lib
 
 class SparseConvFunction(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, features: torch.Tensor, weights: torch.Tensor, pack_impl, transposed: bool):
+    def forward(ctx, features: torch.Tensor, weights: torch.Tensor, pack_impl, transposed: bool, bias=None):
         C = _lib.load()
-        y, wkio = C.conv_forward(features, weights, pack_impl, transposed)
+        y, wkio = C.conv_forward(features, weights, pack_impl, transposed, bias)
         ctx.save_for_backward(features, wkio)
         ctx.pack_impl = pack_impl
         ctx.transposed = transposed
+        ctx.bias_dtype = bias.dtype if bias is not None else None
         return y
 
     @staticmethod
     def backward(ctx, grad_out: torch.Tensor):
         C = _lib.load()
         features, wkio = ctx.saved_tensors
-        need_dx, need_dw = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
-        if grad_out is None or not (need_dx or need_dw):
-            return None, None, None, None
-        dx, dw = C.conv_backward(grad_out, features, wkio, ctx.pack_impl, ctx.transposed, need_dx, need_dw)
-        return (dx if need_dx else None), (dw if need_dw else None), None, None
+        need_dx, need_dw, need_db = ctx.needs_input_grad[0], ctx.needs_input_grad[1], ctx.needs_input_grad[4]
+        if grad_out is None or not (need_dx or need_dw or need_db):
+            return None, None, None, None, None
+        dx = dw = None
+        if need_dx or need_dw:
+            dx, dw = C.conv_backward(grad_out, features, wkio, ctx.pack_impl, ctx.transposed, need_dx, need_dw)
+        db = grad_out.sum(0, dtype=torch.float32).to(ctx.bias_dtype) if need_db else None
+        return (dx if need_dx else None), (dw if need_dw else None), None, None, db
 
 
-def sparse_conv(features: torch.Tensor, weights: torch.Tensor, pack_impl, transposed: bool) -> torch.Tensor:
-    return SparseConvFunction.apply(features, weights, pack_impl, transposed)
+def sparse_conv(features: torch.Tensor, weights: torch.Tensor, pack_impl, transposed: bool, bias=None) -> torch.Tensor:
+    """One sparse convolution with autograd; `bias` ([C_out], optional) is added in the contraction's
+    epilogue on the tensor-core path (one pass over the output instead of two)."""
+    return SparseConvFunction.apply(features, weights, pack_impl, transposed, bias)

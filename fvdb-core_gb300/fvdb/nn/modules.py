@@ -93,10 +93,8 @@ class SparseConv3d(nn.Module):
         if self.training:
             kmap.build_implicit_gemm(sorted=False, training=False)
         prec = None if self.precision == "native" else self.precision
-        if not self.transposed:
-            out_feature = kmap.sparse_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM, precision=prec)
-        else:
-            out_feature = kmap.sparse_transpose_conv_3d(in_feature, self.weight, ConvPackBackend.IGEMM, precision=prec)
+        # the bias is added in the contraction's epilogue (the reference adds it in a second pass)
+        out_feature = kmap._conv_with_bias(in_feature, self.weight, self.bias, self.transposed, prec)
         return out_grid, out_feature, out_kmap
 
     def forward(self, input: VDBTensor, out_grid: Optional[GridBatch] = None) -> VDBTensor:
@@ -104,10 +102,10 @@ class SparseConv3d(nn.Module):
         if self.kernel_size == (1, 1, 1) and self.stride == (1, 1, 1):
             out_feature = in_feature.jagged_like(in_feature.jdata.matmul(self.weight.transpose(0, 1)))
             out_grid, out_kmap = in_grid, in_kmap
+            if self.bias is not None:
+                out_feature.jdata = out_feature.jdata + self.bias
         else:
             out_grid, out_feature, out_kmap = self._dispatch_conv(in_feature, in_grid, in_kmap, out_grid)
-        if self.bias is not None:
-            out_feature.jdata = out_feature.jdata + self.bias
         if out_grid is None:
             raise ValueError("Failed to compute output grid. This is a bug in the implementation.")
         return VDBTensor(out_grid, out_feature, out_kmap)

@@ -50,16 +50,18 @@ def _vec(v) -> list[int]:
     return v * 3 if len(v) == 1 else v
 
 
-def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, precision: str | None) -> torch.Tensor:
+def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, precision: str | None,
+           bias: torch.Tensor | None = None) -> torch.Tensor:
     if precision in (None, "native"):
-        return sparse_conv(data, weights, impl, transposed)
+        return sparse_conv(data, weights, impl, transposed, bias)
     if precision == "bf16":
-        return sparse_conv(data.to(torch.bfloat16), weights.to(torch.bfloat16), impl, transposed)
+        return sparse_conv(data.to(torch.bfloat16), weights.to(torch.bfloat16), impl, transposed, bias)
     if precision == "fp8":
-        if torch.is_grad_enabled() and (data.requires_grad or weights.requires_grad):
+        if torch.is_grad_enabled() and (data.requires_grad or weights.requires_grad or
+                                        (bias is not None and bias.requires_grad)):
             raise RuntimeError("the FP8 convolution is forward-only; use precision='bf16' for training")
         y, _, _ = _lib.load().conv_forward_fp8(data, weights, impl, transposed)
-        return y
+        return y if bias is None else y + bias.to(y.dtype)
     raise ValueError(f"precision must be one of None, 'native', 'bf16', 'fp8' (got {precision!r})")
 
 
@@ -155,6 +157,16 @@ class SparseConvPackInfo:
         data = self._features(input, tgt.grid_count, tgt.total_voxels)
         out = _apply(data, weights, self._impl, True, precision)
         return JaggedTensor.from_data_and_offsets(out, self._impl.source_grid.joffsets)
+
+    def _conv_with_bias(self, input, weights: torch.Tensor, bias: torch.Tensor | None, transposed: bool,
+                        precision: str | None = None) -> JaggedTensor:
+        """sparse_conv_3d / sparse_transpose_conv_3d plus a per-output-channel bias added in the
+        contraction's epilogue (used by nn.SparseConv3d)."""
+        src, tgt = self._impl.source_grid, self._impl.target_grid
+        inp, out = (tgt, src) if transposed else (src, tgt)
+        data = self._features(input, inp.grid_count, inp.total_voxels)
+        y = _apply(data, weights, self._impl, transposed, precision, bias)
+        return JaggedTensor.from_data_and_offsets(y, out.joffsets)
 
     # ---------------------------------------------------------------- devices -----------
     def to(self, to_device) -> "SparseConvPackInfo":

@@ -310,6 +310,18 @@ int fvgb_conv_fwd_tc(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, in
                      void *y, int64_t ldy, const float *out_scale, int32_t *err_dev, fvgb_stream_t stream);
 
 /*
+ * fvgb_conv_fwd_tc with a per-output-channel FP32 bias added in the epilogue (after out_scale,
+ * before the BF16 rounding): y[m, :] = out_scale (.) sum_k ... + bias.  bias may be null (then
+ * identical to fvgb_conv_fwd_tc).  Rows of tiles without any active offset get the bias alone.
+ * No counterpart in the reference, which adds the bias as a separate pass over the output
+ * (fvdb/nn/modules.py:399-400).
+ */
+int fvgb_conv_fwd_tc_bias(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx, const int32_t *map,
+                          int64_t n_out, int32_t K, const uint32_t *tile_mask, const void *packed_w, int32_t c_out,
+                          void *y, int64_t ldy, const float *out_scale, const float *bias, int32_t *err_dev,
+                          fvgb_stream_t stream);
+
+/*
  * Tensor-core weight gradient, BF16 operands:  dw[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co]
  * (FP32, [K, c_in, c_out] contiguous).  c_in in {32, 64, 128} (128/c_in offsets share one
  * M=128 MMA), c_out in {64, 128, 256}; rows of x and dy 16-byte aligned.  Per-CTA FP32
