@@ -149,9 +149,10 @@ def useful_flops(p1, p2, cin1=32, cout1=64, cin2=64, cout2=64) -> tuple[float, i
     return 2.0 * (P1 * cin1 * cout1 + P2 * cin2 * cout2), P1, P2
 
 
-# DRAM bytes (read + write) of one layer-1 contraction launch per voxel, from the ncu capture
-# summarised in profiles/conv_tc_fwd_l1_830k_full.md: (142.95 + 70.46) MB over 829,865 voxels
-# of the same workload generator at 500k points per grid; traffic grows with the voxel count.
+# DRAM bytes (read + write) of one layer-1 contraction launch per voxel, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of one launch on the same workload generator
+# at 500k points per grid: (142.95 + 70.46) MB over 829,865 voxels; traffic grows with the
+# voxel count.
 L1_DRAM_BYTES_PER_VOXEL = (142.949e6 + 70.459e6) / 829_865
 
 
@@ -577,6 +578,17 @@ def leg_train(fvdb, dev, args) -> dict:
     res["bf16"]["errors_vs_fp64_same_rounding"] = {
         "y": rel_errors(outs["bf16"][0], bf(y2.detach())), "dx": rel_errors(outs["bf16"][1], bf(dxq)),
         "dw1": rel_errors(outs["bf16"][2], bf(dw1q))}
+    # FP64 arithmetic on BF16-rounded x, W1, W2 and dy with no other rounding, against FP64 on the
+    # unrounded inputs: the input rounding alone moves pre-activations near zero across the ReLU
+    # (round-to-nearest never changes the sign of a rounded output), so this shows how much of the
+    # stack's gradient error the inputs' rounding accounts for.
+    xr = x0.to(dev).bfloat16().double().requires_grad_(True)
+    w1r = w1.to(dev).bfloat16().double().requires_grad_(True)
+    yr = pack.sparse_conv_3d(torch.relu(pack.sparse_conv_3d(xr, w1r).jdata), w2.to(dev).bfloat16().double()).jdata
+    dxr, dw1r = torch.autograd.grad(yr, (xr, w1r), dy.to(dev).bfloat16().double())
+    res["fp64_on_bf16_rounded_inputs_vs_fp64"] = {
+        "y": rel_errors(yr.detach(), outs["fp64"][0]), "dx": rel_errors(dxr, outs["fp64"][1]),
+        "dw1": rel_errors(dw1r, outs["fp64"][2])}
     # One SparseConv3d (3^3, 64->64) forward + backward, BF16 vs FP64 on the unrounded inputs:
     # without a ReLU between layers no mask can flip, so this is the layer's own BF16 error.
     one = {}

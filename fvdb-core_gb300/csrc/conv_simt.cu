@@ -322,13 +322,17 @@ extern "C" int fvgb_conv_wgrad_simt_noalloc(int32_t dtype, const void *x, int64_
     if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldm < K || ldx < c_in || lddy < c_out || !dw)
         return FVGB_EINVAL;
     if (dtype != FVGB_F32 && dtype != FVGB_F64) return FVGB_ETYPE;
+    if (K > 65535) return FVGB_EINVAL;  // one grid row per kernel offset
     const size_t elem = dtype == FVGB_F64 ? 8 : 4;
-    const size_t per_chunk_bytes = (size_t)K * (size_t)c_in * (size_t)c_out * elem;
-    const int64_t cap_chunks = (int64_t)(kWgradScratchBytes / per_chunk_bytes);
-    if (cap_chunks < 1) {
+    // K*c_in*c_out*elem <= the array, compared without overflow: K*c_in < 2^47 fits int64, and
+    // for integers a*b > c  <=>  a > floor(c / b)
+    const int64_t kc = (int64_t)K * c_in;
+    if (kc > (int64_t)(kWgradScratchBytes / ((size_t)c_out * elem))) {
         record_message("fvgb_conv_wgrad_simt_noalloc: K*c_in*c_out partials exceed the 4 MiB scratch array");
         return FVGB_ENOSPACE;
     }
+    const size_t per_chunk_bytes = (size_t)kc * (size_t)c_out * elem;
+    const int64_t cap_chunks = (int64_t)(kWgradScratchBytes / per_chunk_bytes);
     void *scratch = nullptr;
     const int st = wgrad_scratch_address(&scratch);
     if (st != FVGB_OK) return st;

@@ -5,6 +5,9 @@
 // Reference behaviour replaced: dispatchCreateNanoGridFromIJK<kCUDA>
 // (src/fvdb/detail/ops/BuildGridFromIjk.cu:26-83), which loops over the grids on the
 // host and calls nanovdb::tools::cuda::voxelsToGrid per grid.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include <cub/cub.cuh>
 
 #include "common.cuh"
@@ -211,20 +214,45 @@ __global__ void leaf_finish_kernel(FvgbLeaf *__restrict__ leaves, int64_t L, int
     }
 }
 
-__global__ void points_kernel(const float *__restrict__ pts, const int64_t *__restrict__ joff,
-                              int32_t B, int64_t n, const double *__restrict__ vs,
-                              const double *__restrict__ org, int32_t *__restrict__ out) {
+// One coordinate of VoxelCoordTransform(1/w, -o/w).apply(p).round() in the arithmetic type T
+// that the reference uses for the points' dtype (opmath: double for FP64 points, float for
+// FP32/FP16/BF16): scale and translation are the double quotients rounded once to T, the
+// transform is one fused multiply-add in T, and round() is floor(v + 1/2) in T
+// (src/fvdb/detail/VoxelCoordTransform.h:86-110,230-330, BuildGridFromPoints.cu:27-43).
+template <typename T>
+__device__ __forceinline__ int32_t voxelise(T p, double w, double o);
+template <>
+__device__ __forceinline__ int32_t voxelise<float>(float p, double w, double o) {
+    const float s = (float)(1.0 / w), t = (float)(-o / w);
+    return (int32_t)floorf(__fadd_rn(__fmaf_rn(p, s, t), 0.5f));
+}
+template <>
+__device__ __forceinline__ int32_t voxelise<double>(double p, double w, double o) {
+    const double s = 1.0 / w, t = -o / w;
+    return (int32_t)floor(__dadd_rn(__fma_rn(p, s, t), 0.5));
+}
+
+template <typename P>
+__device__ __forceinline__ float point_as_float(P v) { return (float)v; }
+template <>
+__device__ __forceinline__ float point_as_float<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <>
+__device__ __forceinline__ float point_as_float<__half>(__half v) { return __half2float(v); }
+
+// P: storage type of the points; T: arithmetic type (double for FP64 points, else float).
+template <typename P, typename T>
+__global__ void points_kernel(const P *__restrict__ pts, const int64_t *__restrict__ joff, int32_t B, int64_t n,
+                              const double *__restrict__ vs, const double *__restrict__ org,
+                              int32_t *__restrict__ out) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int32_t b = batch_of(joff, B, i);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        // VoxelCoordTransform(1/w, -o/w).apply(p).round() in the points' precision
-        // (src/fvdb/detail/VoxelCoordTransform.h:320-333, BuildGridFromPoints.cu:37-41)
-        const float inv = (float)(1.0 / vs[3 * b + a]);
-        const float tr = (float)(-org[3 * b + a] / vs[3 * b + a]);
-        const float v = pts[3 * i + a] * inv + tr;
-        out[3 * i + a] = (int32_t)floorf(v + 0.5f);
+        T v;
+        if constexpr (sizeof(T) == 8) v = (T)pts[3 * i + a];
+        else v = point_as_float<P>(pts[3 * i + a]);
+        out[3 * i + a] = voxelise<T>(v, vs[3 * b + a], org[3 * b + a]);
     }
 }
 
@@ -433,14 +461,31 @@ extern "C" int fvgb_grid_index_build(const FvgbGrid *g, const int32_t *leaf_ids,
     return launch_status();
 }
 
-extern "C" int fvgb_points_to_ijk(const float *points, const int64_t *joffsets, int32_t num_grids,
+extern "C" int fvgb_points_to_ijk(int32_t dtype, const void *points, const int64_t *joffsets, int32_t num_grids,
                                   int64_t n, const double *voxel_sizes, const double *origins,
                                   int32_t *out_ijk, fvgb_stream_t stream) {
-    if (n < 0 || num_grids < 1 || (n > 0 && (!points || !out_ijk || !voxel_sizes || !origins)))
+    if (dtype != FVGB_F32 && dtype != FVGB_F64 && dtype != FVGB_F16 && dtype != FVGB_BF16) return FVGB_ETYPE;
+    if (n < 0 || num_grids < 1 || (n > 0 && (!points || !out_ijk || !voxel_sizes || !origins || !joffsets)))
         return FVGB_EINVAL;
     if (n == 0) return FVGB_OK;
-    points_kernel<<<blocks_for(n), kThreads, 0, as_stream(stream)>>>(points, joffsets, num_grids, n,
-                                                                     voxel_sizes, origins, out_ijk);
+    cudaStream_t s = as_stream(stream);
+    switch (dtype) {
+        case FVGB_F64:
+            points_kernel<double, double><<<blocks_for(n), kThreads, 0, s>>>(
+                (const double *)points, joffsets, num_grids, n, voxel_sizes, origins, out_ijk);
+            break;
+        case FVGB_F16:
+            points_kernel<__half, float><<<blocks_for(n), kThreads, 0, s>>>(
+                (const __half *)points, joffsets, num_grids, n, voxel_sizes, origins, out_ijk);
+            break;
+        case FVGB_BF16:
+            points_kernel<__nv_bfloat16, float><<<blocks_for(n), kThreads, 0, s>>>(
+                (const __nv_bfloat16 *)points, joffsets, num_grids, n, voxel_sizes, origins, out_ijk);
+            break;
+        default:
+            points_kernel<float, float><<<blocks_for(n), kThreads, 0, s>>>(
+                (const float *)points, joffsets, num_grids, n, voxel_sizes, origins, out_ijk);
+    }
     count_launches(1);
     return launch_status();
 }

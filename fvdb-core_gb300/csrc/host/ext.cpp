@@ -79,6 +79,18 @@ Vec3 to_vec3(const std::vector<int64_t> &x, const char *name) {
     return r;
 }
 
+// Element type code of a feature or point tensor.
+int32_t fvgb_dtype(const Tensor &t) {
+    switch (t.scalar_type()) {
+        case torch::kFloat32: return FVGB_F32;
+        case torch::kFloat64: return FVGB_F64;
+        case torch::kBFloat16: return FVGB_BF16;
+        case torch::kFloat16: return FVGB_F16;
+        default: TORCH_CHECK_TYPE(false, "unsupported feature dtype ", t.scalar_type());
+    }
+    return -1;
+}
+
 // ------------------------------------------------------------------------------------------
 struct GridImpl {
     int64_t B = 0, N = 0, L = 0, cap = 0;
@@ -232,12 +244,13 @@ GridPtr grid_from_points(const Tensor &points, const Tensor &joffsets, const Ten
     TORCH_CHECK_VALUE(points.dim() == 2 && points.size(1) == 3, "points must have shape (N, 3)");
     TORCH_CHECK_TYPE(points.is_floating_point(), "points must have a floating point dtype");
     const int64_t B = joffsets.size(0) - 1;
-    Tensor p = points.to(torch::kFloat32).contiguous();
+    // voxelised in the points' own precision (FP64 in double, the rest in float), as the reference
+    Tensor p = points.contiguous();
     Tensor joff = joffsets.to(points.device(), torch::kInt64).contiguous();
     Tensor vsb = per_grid_vec(vs, B, "voxel_sizes"), orb = per_grid_vec(org, B, "origins");
     Tensor vsd = vsb.to(points.device()), ord = orb.to(points.device());
     Tensor ijk = torch::empty({p.size(0), 3}, torch::dtype(torch::kInt32).device(points.device()));
-    check_status(fvgb_points_to_ijk(p.data_ptr<float>(), joff.data_ptr<int64_t>(), (int32_t)B, p.size(0),
+    check_status(fvgb_points_to_ijk(fvgb_dtype(p), p.data_ptr(), joff.data_ptr<int64_t>(), (int32_t)B, p.size(0),
                                     vsd.data_ptr<double>(), ord.data_ptr<double>(), ijk.data_ptr<int32_t>(),
                                     cur_stream()),
                  "points to ijk");
@@ -521,16 +534,6 @@ void pack_build_implicit_gemm(PackPtr p, bool sorted, int64_t split, bool traini
 
 // ------------------------------------------------------------------------------------------
 // Contractions.  W is viewed as [K, Cin, Cout] (any strides).
-int32_t fvgb_dtype(const Tensor &t) {
-    switch (t.scalar_type()) {
-        case torch::kFloat32: return FVGB_F32;
-        case torch::kFloat64: return FVGB_F64;
-        case torch::kBFloat16: return FVGB_BF16;
-        case torch::kFloat16: return FVGB_F16;
-        default: TORCH_CHECK_TYPE(false, "unsupported feature dtype ", t.scalar_type());
-    }
-    return -1;
-}
 
 // Device flag that the tensor-core kernels raise when a bounded wait gives up (per device).
 Tensor &device_error_flag(const torch::Device &dev) {

@@ -36,7 +36,11 @@ class SparseConvFunction(torch.autograd.Function):
         dx = dw = None
         if need_dx or need_dw:
             dx, dw = C.conv_backward(grad_out, features, wkio, ctx.pack_impl, ctx.transposed, need_dx, need_dw)
-        db = grad_out.sum(0, dtype=torch.float32).to(ctx.bias_dtype) if need_db else None
+        # bias gradient = column sum of dy, accumulated in at least FP32 (FP64 stays FP64)
+        db = None
+        if need_db:
+            acc = torch.promote_types(grad_out.dtype, torch.float32)
+            db = grad_out.sum(0, dtype=acc).to(ctx.bias_dtype)
         return (dx if need_dx else None), (dw if need_dw else None), None, None, db
 
 

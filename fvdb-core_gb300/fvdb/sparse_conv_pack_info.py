@@ -52,17 +52,25 @@ def _vec(v) -> list[int]:
 
 def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, precision: str | None,
            bias: torch.Tensor | None = None) -> torch.Tensor:
+    """One convolution in the requested arithmetic.  The result has the dtype that the
+    reference's `conv(x) + bias` has (torch type promotion of the contraction's output and the
+    bias): the bias is fused into the contraction's epilogue when that dtype is the output's
+    own, and added afterwards (promoting) otherwise."""
     if precision in (None, "native"):
-        return sparse_conv(data, weights, impl, transposed, bias)
-    if precision == "bf16":
-        return sparse_conv(data.to(torch.bfloat16), weights.to(torch.bfloat16), impl, transposed, bias)
-    if precision == "fp8":
+        x, w = data, weights
+    elif precision == "bf16":
+        x, w = data.to(torch.bfloat16), weights.to(torch.bfloat16)
+    elif precision == "fp8":
         if torch.is_grad_enabled() and (data.requires_grad or weights.requires_grad or
                                         (bias is not None and bias.requires_grad)):
             raise RuntimeError("the FP8 convolution is forward-only; use precision='bf16' for training")
         y, _, _ = _lib.load().conv_forward_fp8(data, weights, impl, transposed)
-        return y if bias is None else y + bias.to(y.dtype)
-    raise ValueError(f"precision must be one of None, 'native', 'bf16', 'fp8' (got {precision!r})")
+        return y if bias is None else y + bias
+    else:
+        raise ValueError(f"precision must be one of None, 'native', 'bf16', 'fp8' (got {precision!r})")
+    if bias is not None and torch.result_type(x, bias) != x.dtype:
+        return sparse_conv(x, w, impl, transposed, None) + bias
+    return sparse_conv(x, w, impl, transposed, bias)
 
 
 class SparseConvPackInfo:

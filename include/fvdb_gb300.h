@@ -146,11 +146,15 @@ int fvgb_ijk_to_index(const FvgbGrid *grid, const int32_t *ijk, const int64_t *j
                       int32_t cumulative, int64_t *out, fvgb_stream_t stream);
 
 /*
- * ijk of points: ijk = floor(p / voxel_size - origin / voxel_size + 0.5) per grid,
- * points f32 [n,3], per-grid voxel_size/origin f64 [num_grids,3] (device), batch of
- * each point from joffsets.  Replaces ijkForPoints (src/fvdb/detail/ops/BuildGridFromPoints.cu:27-43).
+ * ijk of points, per grid: ijk = floor(fma(p, s, t) + 1/2) with s = 1/voxel_size and
+ * t = -origin/voxel_size, evaluated in the points' own arithmetic type as the reference does
+ * (at::opmath_type: double for FVGB_F64 points; float for FVGB_F32, FVGB_F16 and FVGB_BF16
+ * points, with s and t rounded once to float).  points [n,3] of `dtype`; per-grid
+ * voxel_size/origin f64 [num_grids,3] (device); the grid of each point from joffsets.
+ * Replaces ijkForPoints + VoxelCoordTransform::apply(...).round()
+ * (src/fvdb/detail/ops/BuildGridFromPoints.cu:27-43, src/fvdb/detail/VoxelCoordTransform.h:86-110).
  */
-int fvgb_points_to_ijk(const float *points, const int64_t *joffsets, int32_t num_grids, int64_t n,
+int fvgb_points_to_ijk(int32_t dtype, const void *points, const int64_t *joffsets, int32_t num_grids, int64_t n,
                        const double *voxel_sizes, const double *origins, int32_t *out_ijk,
                        fvgb_stream_t stream);
 

@@ -19,6 +19,9 @@
  *   - the kernel map  src/fvdb/detail/ops/convolution/pack_info/ConvolutionKernelMap.cu:60-102
  *   - conv_grid       src/fvdb/detail/ops/BuildGridForConv.cu:25-64,190-255
  *                     src/fvdb/detail/ops/CoarseIjkForFineGrid.cu:19-41
+ *   - ijk of points   src/fvdb/detail/ops/BuildGridFromPoints.cu:27-43 with
+ *                     VoxelCoordTransform::apply(...).round()
+ *                     (src/fvdb/detail/VoxelCoordTransform.h:86-110,230-330)
  *
  * Parity of raw map integers against the reference's NanoVDB build is pinned only
  * within one root tile (all coordinates in [0,4096)^3); across root tiles it
@@ -252,4 +255,37 @@ void orc_scatter_add_f64(int64_t n, int64_t c, const double *buf, double *dst, c
         const double *s = buf + i * c;
         for (int64_t j = 0; j < c; ++j) d[j] += s[j];
     }
+}
+
+/*
+ * ijk of points (BuildGridFromPoints.cu:27-43): per axis VoxelCoordTransform(1/w, -o/w)
+ * .apply(p).round() in the points' arithmetic type (opmath_type: double for double points,
+ * float otherwise).  The transform's float copy holds (float)(1/w) and (float)(-o/w)
+ * (VoxelCoordTransform.h:230-240); apply() is p*scale + translate, which nvcc contracts to
+ * one fused multiply-add; NanoVDB's Vec3::round() is Floor(v + 0.5) in the same type.
+ * points are given as double; the f32 variant first rounds each to float (exact for points
+ * that are float, half or bfloat16 values).
+ */
+void orc_points_to_ijk_f32(const double *pts, const int64_t *joff, int32_t B, const double *vs,
+                           const double *org, int32_t *out) {
+    for (int32_t b = 0; b < B; ++b)
+        for (int64_t i = joff[b]; i < joff[b + 1]; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const float s = (float)(1.0 / vs[3 * b + a]);
+                const float t = (float)(-org[3 * b + a] / vs[3 * b + a]);
+                const float v = fmaf((float)pts[3 * i + a], s, t);
+                out[3 * i + a] = (int32_t)floorf(v + 0.5f);
+            }
+}
+
+void orc_points_to_ijk_f64(const double *pts, const int64_t *joff, int32_t B, const double *vs,
+                           const double *org, int32_t *out) {
+    for (int32_t b = 0; b < B; ++b)
+        for (int64_t i = joff[b]; i < joff[b + 1]; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const double s = 1.0 / vs[3 * b + a];
+                const double t = -org[3 * b + a] / vs[3 * b + a];
+                const double v = fma(pts[3 * i + a], s, t);
+                out[3 * i + a] = (int32_t)floor(v + 0.5);
+            }
 }

@@ -7,6 +7,8 @@ Contents (reference paths relative to the fvdb-core tree):
   grid_from_ijk        voxel index order of BuildGridFromIjk.cu:26-83 (fvdb_oracle.c)
   kernel_map           ConvolutionKernelMap.cu:60-102 (fvdb_oracle.c)
   conv_grid            BuildGridForConv.cu:190-255 + CoarseIjkForFineGrid.cu:19-41
+  points_to_ijk        BuildGridFromPoints.cu:27-43 + VoxelCoordTransform.h:86-110 (apply().round()
+                       in the points' precision; fvdb_oracle.c)
   transpose_map        IGEMMBitOperations.cu:92-105
   neighbour_map        SparseConvPackInfo.cpp:61-88 (kmap.t(), nonzero, sizes)
   gs_forward/backward  the reference CPU gather -> torch::mm -> scatter path,
@@ -49,6 +51,10 @@ def _lib():
         L.orc_conv_grid_candidates.argtypes = [P, P, i32, P, P, P, P]
         L.orc_transpose_map.restype = None
         L.orc_transpose_map.argtypes = [P, i64, i64, i64, P, i64]
+        for name in ("orc_points_to_ijk_f32", "orc_points_to_ijk_f64"):
+            f = getattr(L, name)
+            f.restype = None
+            f.argtypes = [P, P, i32, P, P, P]
         for name in ("orc_gather_f32", "orc_scatter_add_f32", "orc_gather_f64", "orc_scatter_add_f64"):
             f = getattr(L, name)
             f.restype = None
@@ -68,6 +74,21 @@ def _vec3(v) -> np.ndarray:
 
 
 # ----------------------------------------------------------------------- integer path ---
+def points_to_ijk(points: np.ndarray, joff, voxel_sizes, origins, precision: str) -> np.ndarray:
+    """ijk of points as the reference voxelises them (BuildGridFromPoints.cu:27-43):
+    precision "f64" for FP64 point clouds, "f32" for FP32 / FP16 / BF16 ones (values given
+    as float64 arrays holding the points' exact values).  voxel_sizes / origins: [B, 3]."""
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    joff = np.ascontiguousarray(joff, dtype=np.int64)
+    B = joff.shape[0] - 1
+    vs = np.ascontiguousarray(np.broadcast_to(np.asarray(voxel_sizes, np.float64), (B, 3)))
+    org = np.ascontiguousarray(np.broadcast_to(np.asarray(origins, np.float64), (B, 3)))
+    out = np.empty((pts.shape[0], 3), dtype=np.int32)
+    f = _lib().orc_points_to_ijk_f64 if precision == "f64" else _lib().orc_points_to_ijk_f32
+    f(_p(pts), _p(joff), B, _p(vs), _p(org), _p(out))
+    return out
+
+
 def grid_from_ijk(ijk: np.ndarray, joff: np.ndarray):
     """(sorted unique ijk [N,3] int32, offsets [B+1] int64) in NanoVDB voxel order."""
     ijk = np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1, 3)

@@ -25,7 +25,7 @@ def _oracle_forward(grid, x, w, b):
     return y + b.detach().double().cpu().numpy()[None, :]
 
 
-@pytest.mark.parametrize("dtype,tol", [(torch.bfloat16, 1e-2), (torch.float32, 1e-5)])
+@pytest.mark.parametrize("dtype,tol", [(torch.bfloat16, 1e-2), (torch.float32, 1e-5), (torch.float64, 1e-12)])
 def test_module_bias(cuda_device, dtype, tol):
     import fvdb
 
@@ -49,7 +49,24 @@ def test_module_bias(cuda_device, dtype, tol):
     assert torch.equal(x.grad, x2.grad)
     assert torch.equal(conv.weight.grad, plain.weight.grad)
     db = dy.double().sum(0)
+    assert conv.bias.grad.dtype == dtype
     assert rel_l2(conv.bias.grad.double().cpu().numpy(), db.cpu().numpy()) <= tol
+
+
+def test_output_dtype_follows_promotion(cuda_device):
+    """precision='bf16' on an FP32 module: the output is FP32, as the reference's conv(x) + bias
+    (the bias is then added after the BF16 contraction instead of in its epilogue)."""
+    import fvdb
+
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(random_sparse_ijk(3000, 24, 9)).to(cuda_device))
+    torch.manual_seed(2)
+    conv = fvdb.nn.SparseConv3d(32, 64, 3, bias=True).to(cuda_device)
+    conv.precision = "bf16"
+    x = torch.randn(grid.total_voxels, 32, device=cuda_device)
+    y = conv(fvdb.nn.VDBTensor(grid, grid.jagged_like(x))).data.jdata
+    assert y.dtype == torch.float32
+    ref = _oracle_forward(grid, x.bfloat16().float(), conv.weight.bfloat16().float(), conv.bias)
+    assert rel_l2(y.detach().double().cpu().numpy(), ref) <= 1e-2
 
 
 def test_bias_alone_where_no_offset_is_active(cuda_device):
@@ -60,8 +77,11 @@ def test_bias_alone_where_no_offset_is_active(cuda_device):
     pack, _ = src.sparse_conv_kernel_map(3, 1, target_grid=tgt)
     x = torch.randn(src.total_voxels, 32, device=cuda_device).bfloat16()
     w = torch.randn(64, 32, 3, 3, 3, device=cuda_device).bfloat16()
-    b = torch.randn(64, device=cuda_device)
+    b = torch.randn(64, device=cuda_device).bfloat16()  # same dtype: fused into the epilogue
     y = pack._conv_with_bias(x, w, b, False).jdata
     torch.cuda.synchronize()
-    assert y.shape == (tgt.total_voxels, 64)
-    assert torch.equal(y, b.bfloat16()[None, :].expand_as(y))
+    assert y.shape == (tgt.total_voxels, 64) and y.dtype == torch.bfloat16
+    assert torch.equal(y, b[None, :].expand_as(y))
+    b32 = b.float()  # promotes: added after the contraction, FP32 output
+    y32 = pack._conv_with_bias(x, w, b32, False).jdata
+    assert y32.dtype == torch.float32 and torch.equal(y32, b32[None, :].expand_as(y32))

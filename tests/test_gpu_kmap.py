@@ -179,6 +179,34 @@ def test_from_points_and_empty(fvdb, cuda_device):
     assert pack.out_in_map.shape[0] == 0
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32, torch.float16])
+def test_from_points_rounds_in_point_precision(fvdb, cuda_device, dtype):
+    """Points on and a few ulps next to half-voxel boundaries, two grids with their own voxel
+    sizes and origins: the voxels are bit-exact vs the oracle's voxelisation in the points'
+    own precision (double for FP64, float for FP32 / FP16), as BuildGridFromPoints.cu:27-43."""
+    from tests.test_points_oracle import boundary_points
+
+    w, o = [0.1, 0.05], [0.0, 0.37]
+    parts = [boundary_points(3000, w[b], o[b], 11 + b) for b in range(2)]
+    pts64 = np.concatenate(parts)
+    pts = torch.from_numpy(pts64).to(dtype)
+    vals = pts.double().numpy()  # the exact values the device sees
+    joff = np.array([0, parts[0].shape[0], pts64.shape[0]])
+    vs = np.array([[w[0]] * 3, [w[1]] * 3])
+    org = np.array([[o[0]] * 3, [o[1]] * 3])
+    prec = "f64" if dtype == torch.float64 else "f32"
+    o_pts = orc.points_to_ijk(vals, joff, vs, org, prec)
+    o_ijk, o_off = orc.grid_from_ijk(o_pts, joff)
+    jt = fvdb.JaggedTensor.from_data_and_offsets(pts.to(cuda_device), torch.from_numpy(joff).to(cuda_device))
+    grid = fvdb.GridBatch.from_points(jt, voxel_sizes=torch.from_numpy(vs), origins=torch.from_numpy(org))
+    assert np.array_equal(grid.ijk.jdata.cpu().numpy(), o_ijk)
+    assert np.array_equal(grid.joffsets.cpu().numpy(), o_off)
+    if dtype == torch.float64:
+        # the float rule places some of these points in other voxels
+        f_pts = orc.points_to_ijk(vals.astype(np.float32).astype(np.float64), joff, vs, org, "f32")
+        assert (f_pts != o_pts).any()
+
+
 def test_coordinate_range_is_checked(fvdb, cuda_device):
     bad = torch.tensor([[0, 0, 0], [1 << 21, 0, 0]], dtype=torch.int32, device=cuda_device)
     with pytest.raises(ValueError):

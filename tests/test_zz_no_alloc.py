@@ -41,7 +41,11 @@ def _p(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-@pytest.mark.parametrize("dtype,code,cin,cout", [(torch.float32, F32, 16, 32), (torch.float64, F64, 24, 8)])
+# (64, 64) FP32: one row chunk's partials take 27*64*64*4 = 442 KB, so the 4 MiB array holds 9
+# chunks against the 47 that the allocating entry point plans for 12k voxels; the no-alloc
+# entry point then re-plans with longer row chunks.
+@pytest.mark.parametrize("dtype,code,cin,cout", [(torch.float32, F32, 16, 32), (torch.float64, F64, 24, 8),
+                                                 (torch.float32, F32, 64, 64)])
 def test_noalloc_matches_allocating_entry_point(cuda_device, dtype, code, cin, cout):
     from fvdb import _lib
 
@@ -87,3 +91,9 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(cuda_device):
                                           ctypes.c_int64(256), _p(dw), stream)
     assert rc == ENOSPACE
     assert b"4 MiB" in lib.fvgb_last_error()
+    # sizes whose product overflows 64 bits are rejected too, not wrapped into a small size
+    big = 1 << 30
+    rc = lib.fvgb_conv_wgrad_simt_noalloc(F32, _p(x), ctypes.c_int64(n), big, ctypes.c_int64(big), _p(kmap),
+                                          ctypes.c_int64(n), 27, ctypes.c_int64(27), _p(dy), big,
+                                          ctypes.c_int64(big), _p(dw), stream)
+    assert rc == ENOSPACE
