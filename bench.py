@@ -156,10 +156,12 @@ def useful_flops(p1, p2, cin1=32, cout1=64, cin2=64, cout2=64) -> tuple[float, i
 L1_DRAM_BYTES_PER_VOXEL = (142.949e6 + 70.459e6) / 829_865
 
 
-def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) -> tuple[float, bool]:
-    """Layer-1 tcgen05 contraction alone through the C ABI (fvgb_conv_fwd_tc): average launch
-    duration from CUDA events around `launches` back-to-back launches on the current stream,
-    and whether its output is bitwise identical to the same layer run through
+def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) -> dict:
+    """Layer-1 tcgen05 contraction alone through the C ABI: the planned kernel
+    (fvgb_conv_fwd_tc_planned over the pack's tile plan, the one the step runs) and, for
+    comparison, the unplanned kernel (fvgb_conv_fwd_tc over the int32 map).  Average launch
+    durations from CUDA events around `launches` back-to-back launches on the current stream,
+    and whether each output is bitwise identical to the same layer run through
     SparseConvPackInfo.sparse_conv_3d."""
     import ctypes
 
@@ -168,6 +170,7 @@ def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) ->
     tm = p1._impl.tile_mask(False)
     K = kmap.shape[1]
     cout, cin = w1.shape[0], w1.shape[1]
+    plan = p1._impl.tile_plan(False, cin * 2)
     wkio = w1.permute(4, 3, 2, 1, 0).reshape(K, cin, cout).contiguous()
     P = lambda t: ctypes.c_void_p(t.data_ptr())
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -176,26 +179,41 @@ def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) ->
     packed = torch.empty(nb.value, dtype=torch.uint8, device=x.device)
     assert lib.fvgb_tc_pack_weights(2, P(wkio), ctypes.c_int64(K), cin, cout, ctypes.c_int64(cin * cout),
                                     ctypes.c_int64(cout), ctypes.c_int64(1), P(packed), nb, stream) == 0
-    y = torch.empty(n, cout, device=x.device, dtype=torch.bfloat16)
     err = torch.zeros(1, dtype=torch.int32, device=x.device)
+    ref = p1.sparse_conv_3d(x, w1).jdata
 
-    def launch():
+    def planned(y):
+        rc = lib.fvgb_conv_fwd_tc_planned(2, P(x), ctypes.c_int64(n), cin, ctypes.c_int64(x.stride(0)), P(plan),
+                                          ctypes.c_int64(n), K, P(packed), cout, P(y), ctypes.c_int64(cout), None,
+                                          None, P(err), stream)
+        assert rc == 0, rc
+
+    def unplanned(y):
         rc = lib.fvgb_conv_fwd_tc(2, P(x), ctypes.c_int64(n), cin, ctypes.c_int64(x.stride(0)), P(kmap),
                                   ctypes.c_int64(n), K, P(tm) if tm is not None else None, P(packed), cout, P(y),
                                   ctypes.c_int64(cout), None, P(err), stream)
         assert rc == 0, rc
 
-    launch()
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(launches):
-        launch()
-    b.record()
-    torch.cuda.synchronize()
-    assert int(err.item()) == 0
-    identical = bool(torch.equal(p1.sparse_conv_3d(x, w1).jdata, y))
-    return a.elapsed_time(b) / launches, identical
+    def build_plan(_y):
+        rc = lib.fvgb_tc_plan_build(P(kmap), ctypes.c_int64(n), K, cin * 2, P(plan), ctypes.c_size_t(plan.numel()),
+                                    stream)
+        assert rc == 0, rc
+
+    out = {}
+    for name, fn in (("planned", planned), ("unplanned", unplanned), ("plan_build", build_plan)):
+        y = torch.empty(n, cout, device=x.device, dtype=torch.bfloat16)
+        fn(y)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(launches):
+            fn(y)
+        b.record()
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        out[name] = {"ms": a.elapsed_time(b) / launches, "identical_to_step": bool(torch.equal(ref, y))}
+    del out["plan_build"]["identical_to_step"]
+    return out
 
 
 def load_peaks() -> dict:
@@ -374,7 +392,10 @@ def run_gpu(args) -> None:
         torch.cuda.synchronize()  # the last result has reached host memory
         e2e_ms = t0.elapsed_time(t1) / e2e_steps
 
-    kern_ms, kern_identical = kernel_only_l1(lib, p1, x, model.w1, max(args.steps, 3))
+    kern = kernel_only_l1(lib, p1, x, model.w1, max(args.steps, 3))
+    # the step builds its kernel maps every step, so it runs the unplanned kernel (a tile plan is
+    # built only for a map that is used again); the planned kernel is timed beside it
+    kern_ms, kern_identical = kern["unplanned"]["ms"], kern["unplanned"]["identical_to_step"]
     peaks = load_peaks()
     conv1_flops = 2.0 * P1 * 32 * 64
     conv1_bytes = n_vox * 32 * 2 + n_vox * 64 * 2 + 27 * 32 * 64 * 2 + 4 * 27 * n_vox
@@ -414,6 +435,9 @@ def run_gpu(args) -> None:
             "kernel_tflops": conv1_flops / (kern_ms * 1e-3) / 1e12,
             "tensor_frac": conv1_flops / (kern_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
             "layer1_window_ms": conv_ms,
+            "planned_kernel_ms": kern["planned"]["ms"],
+            "planned_output_identical_to_step": kern["planned"]["identical_to_step"],
+            "plan_build_ms": kern["plan_build"]["ms"],
         },
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -421,12 +445,17 @@ def run_gpu(args) -> None:
         line["cpu_baseline"] = {"value": r["flops"] / r["seconds"] / 1e12, "unit": "TFLOP/s", "cores": torch.get_num_threads(),
                                 "kind": "port",
                                 "sample": f"layer 1 (3^3 32->64) of grid 0 restricted to {r['voxels']} voxels, fp32, kernel map + gather/torch.mm/scatter ({r['seconds']:.2f} s)"}
-    if not args.no_extras:
+    legs = set() if args.no_extras else set(args.legs.split(","))
+    if "fp32" in legs:
         line["fp32_plain"] = leg_fp32(fvdb, grid, x, model, flops, args)
-        line["c1_fp32"] = leg_c1(fvdb, dev, args)
         line["bf16_vs_fp32"] = tf / line["fp32_plain"]["value"] if line["fp32_plain"]["value"] else None
+    if "c1" in legs:
+        line["c1_fp32"] = leg_c1(fvdb, dev, args)
+    if "train" in legs:
         line["train_c3"] = leg_train(fvdb, dev, args)
+    if "fp8" in legs:
         line["fp8_c4"] = leg_fp8(fvdb, dev, args)
+    if "serve" in legs:
         line["serving_c5"] = leg_serve(fvdb, dev, args)
     if rank == 0:
         print(json.dumps(line))
@@ -609,18 +638,23 @@ def shell_ijk(target: int, seed: int, device, res_cap: int = 4000) -> torch.Tens
     r = 0.2 + 0.25 * float(torch.rand(1, generator=g))
     c = 0.3 + 0.4 * torch.rand(3, generator=g)
     R = int(min(res_cap, max(16, math.sqrt(target / (1.55 * 4 * math.pi * r * r)))))
-    d = torch.randn(int(target * 2.5), 3, generator=g)
-    p = c + r * d / d.norm(dim=1, keepdim=True)
+    d = torch.randn(int(target * 2.5), 3, generator=g).to(device)
+    p = c.to(device) + r * d / d.norm(dim=1, keepdim=True)
     ijk = torch.floor(p.clamp(0, 1 - 1e-6) * R + 0.5).to(torch.int32)
-    return torch.unique(ijk, dim=0).to(device)
+    return torch.unique(ijk, dim=0)
 
 
 def leg_fp8(fvdb, dev, args) -> dict:
-    """~4M sphere-shell voxels at 1024^3: FP8-E4M3 3^3 conv C128->256 (per-channel scales), then
+    """~4M sphere-shell voxels at 1024^3 (shells added until the union reaches 4M): FP8-E4M3 3^3
+    conv C128->256 (per-channel scales), then
     2^3 stride-2 transposed conv C256->128 from conv_grid(2,2) back onto the fine grid.  Timing
     FP8 and BF16; errors vs FP64 on 4096 sampled output rows."""
-    parts = [shell_ijk(1_000_000, 300 + i, dev, 1024) for i in range(4)]
-    ijk = torch.unique(torch.cat(parts), dim=0)
+    # sphere shells (seeds 300, 301, ...) are added until their union holds ~4M voxels
+    ijk = torch.zeros((0, 3), dtype=torch.int32, device=dev)
+    for i in range(16):
+        ijk = torch.unique(torch.cat([ijk, shell_ijk(1_000_000, 300 + i, dev, 1024)]), dim=0)
+        if ijk.shape[0] >= 4_000_000:
+            break
     grid = fvdb.GridBatch.from_ijk(ijk)
     g = torch.Generator().manual_seed(301)
     x = torch.randn(grid.total_voxels, 128, generator=g).to(dev, torch.bfloat16)
@@ -658,37 +692,67 @@ def leg_fp8(fvdb, dev, args) -> dict:
 
 
 def leg_serve(fvdb, dev, args) -> dict:
-    """Poisson arrivals, N log-uniform [1e4, 2e6] voxels per request (one sphere shell each),
-    4-layer 3^3 stack 32->64->64->32 with ReLU, BF16, continuous batching under an HBM budget;
-    against the plain FP32 per-request form on the same arrival schedule."""
-    from fvdb.serving import ContinuousBatcher, ConvStack, GPUExecutor, Request, latency_stats
+    """Poisson arrivals swept over the requested rates, N log-uniform [1e4, 2e6] voxels per
+    request (one sphere shell each), 4-layer 3^3 stack 32->64->64->32 with ReLU, BF16,
+    continuous batching under an HBM budget; against the plain FP32 per-request form on the
+    same arrival schedule.  The requests of every rate are drawn from one pool of distinct
+    grids (sizes log-uniform) so their host buffers fit in pinned memory; features arrive as
+    BF16 in both forms (the FP32 form computes in FP32).  Errors against the stack in FP64 are
+    stated for a sample of served requests."""
+    from fvdb.serving import ContinuousBatcher, ConvStack, GPUExecutor, Request, latency_stats, run_alone
 
+    rates = [float(r) for r in args.serve_rates.split(",") if r]
     rng = np.random.default_rng(400)
-    reqs = []
-    t = 0.0
-    for i in range(args.serve_requests):
+    pool = []
+    for i in range(args.serve_pool):
         n = int(math.exp(rng.uniform(math.log(1e4), math.log(2e6))))
         ijk = shell_ijk(n, 400 + i, dev).cpu().pin_memory()
         feats = torch.randn(ijk.shape[0], 32, generator=torch.Generator().manual_seed(i)).bfloat16().pin_memory()
-        t += float(rng.exponential(1.0 / args.serve_rate))
-        reqs.append((i, ijk, feats, t))
+        pool.append((ijk, feats))
     model = ConvStack([32, 64, 64, 32], dev, seed=0)
-    out = {"rate_per_s": args.serve_rate, "requests": len(reqs)}
-    # continuous batching (3 streams, up to 4M voxels per jagged batch) vs one request at a time in FP32
-    for name, mdl, slots, per_batch in (("bf16_batched", model, 3, None),
-                                        ("fp32_per_request", model.to_dtype(torch.float32), 1, 1)):
+    model32 = model.to_dtype(torch.float32)
+    out = {"requests_per_rate": args.serve_requests, "distinct_grids": len(pool),
+           "pool_voxels_mean": float(np.mean([p[0].shape[0] for p in pool])), "rates": {}}
+    forms = (("bf16_batched", model, 3, None), ("fp32_per_request", model32, 1, 1))
+    servers = {}
+    for name, mdl, slots, per_batch in forms:
         ex = GPUExecutor(mdl, dev, slots=slots)
-        srv = ContinuousBatcher(ex, hbm_budget=48 << 30, max_batch_voxels=4_000_000, slots=slots,
-                                max_batch_requests=per_batch)
-        batch = [Request(rid=i, ijk=a, features=(f if name.startswith("bf16") else f.float()), arrival=t0)
-                 for i, a, f, t0 in reqs]
-        # warm-up on the first request alone
-        srv.serve([Request(rid=-1, ijk=batch[0].ijk, features=batch[0].features, arrival=0.0)])
-        done = srv.serve(batch)
-        st = latency_stats(done)
-        st["batches"] = srv.batches
-        st["errors"] = sum(1 for r in done if r.error)
-        out[name] = st
+        srv_args = dict(hbm_budget=48 << 30, max_batch_voxels=4_000_000, slots=slots, max_batch_requests=per_batch)
+        servers[name] = (ex, srv_args)
+        # warm-up: one request alone
+        ContinuousBatcher(ex, **srv_args).serve([Request(rid=-1, ijk=pool[0][0], features=pool[0][1], arrival=0.0)])
+    sample_done = {}
+    for ri, rate in enumerate(rates):
+        r2 = np.random.default_rng(1000 + ri)
+        picks = r2.integers(0, len(pool), size=args.serve_requests)
+        arrivals = np.cumsum(r2.exponential(1.0 / rate, size=args.serve_requests))
+        entry = {}
+        for name, mdl, slots, per_batch in forms:
+            ex, srv_args = servers[name]
+            srv = ContinuousBatcher(ex, **srv_args)
+            batch = [Request(rid=i, ijk=pool[int(k)][0], features=pool[int(k)][1], arrival=float(t))
+                     for i, (k, t) in enumerate(zip(picks, arrivals))]
+            done = srv.serve(batch)
+            st = latency_stats(done)
+            st["batches"] = srv.batches
+            st["errors"] = sum(1 for r in done if r.error)
+            entry[name] = st
+            if name == "bf16_batched" and ri == len(rates) - 1:
+                sample_done = {int(picks[r.rid]): r for r in done if r.error is None}
+        out["rates"][str(int(rate) if rate == int(rate) else rate)] = entry
+    # errors of served BF16 outputs (from the mix at the highest rate) against FP64 alone
+    model64 = model.to_dtype(torch.float64)
+    errs = []
+    for k in sorted(sample_done)[: args.serve_error_sample]:
+        r = sample_done[k]
+        y64, ijk64 = run_alone(model64, r, dev)
+        assert torch.equal(ijk64, r.out_ijk)
+        errs.append(rel_errors(r.output, y64))
+    if errs:
+        out["errors_vs_fp64"] = {"requests": len(errs), "rel_l2_max": max(e["rel_l2"] for e in errs),
+                                 "max_rel_to_scale_max": max(e["max_rel_to_scale"] for e in errs)}
+    for ex, _ in servers.values():
+        ex.close()
     return out
 
 
@@ -701,8 +765,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / training / FP8 / serving legs")
-    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson request rate of the serving leg (1/s)")
-    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving leg")
+    ap.add_argument("--legs", default="fp32,c1,train,fp8,serve",
+                    help="comma-separated extra legs to run after the headline step")
+    ap.add_argument("--serve-rates", default="50,100,200,500,1000,2000",
+                    help="Poisson request rates of the serving sweep (1/s)")
+    ap.add_argument("--serve-requests", type=int, default=300, help="requests per rate in the serving leg")
+    ap.add_argument("--serve-pool", type=int, default=40, help="distinct request grids the serving leg draws from")
+    ap.add_argument("--serve-error-sample", type=int, default=4, help="served requests checked against FP64")
     ap.add_argument("--points", type=int, default=2_000_000,
                     help="points per grid (the headline workload uses 2M; smaller only for profiling captures)")
     args = ap.parse_args()

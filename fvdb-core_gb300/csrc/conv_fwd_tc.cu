@@ -21,11 +21,12 @@
 //              into the 128B-swizzled K-major A layout; absent entries (map -1) are zero-stored
 //              with st.shared.  Both are generic-proxy writes, so each warp publishes a stage to
 //              the tensor core (async proxy) itself, kLag stages late: cp.async.wait_group,
-//              fence.proxy.async, __syncwarp, one mbarrier arrive.  The MMA thread never fences
+//              fence.proxy.async, __syncwarp, one mbarrier arrive.  The MMA warp never fences
 //              and its MMAs stream back to back.  Map entries are read before the stage wait so
 //              their latency overlaps it.
-//   warp 8     TMEM allocation (2 x N columns) and the single MMA-issuing thread; tile i
-//              accumulates into TMEM buffer i % 2.
+//   warp 8     TMEM allocation (2 x N columns) and the MMA issuer: the whole warp runs the
+//              issue loop and one elected lane issues each tcgen05.mma; tile i accumulates into
+//              TMEM buffer i % 2.
 //   warps 9-12 epilogue: tcgen05.ld of the finished buffer -> scale -> BF16 -> a shared-memory
 //              copy of the output tile -> one bulk async store of the tile's contiguous rows;
 //              overlaps the next tile's main loop.
@@ -302,9 +303,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
             }
     } else if (warp == kMmaWarp) {
         // ----------------------------------------------------------------- MMA issuer
-        // Descriptors are advanced by constant offsets (16-byte units) from one base: shared
-        // addresses stay below 2^18, so the 14-bit start-address field never carries.
-        if (lane == 0) {
+        // The whole warp runs this loop (warp-uniform control flow, operands in uniform
+        // registers); one elected lane issues each tcgen05 instruction.  Descriptors are
+        // advanced by constant offsets (16-byte units) from one base: shared addresses stay
+        // below 2^18, so the 14-bit start-address field never carries.
+        {
             constexpr uint32_t idesc = EBYTES == 2 ? idesc_m128(BN, 1, 1) : idesc_m128(BN, 0, 0);
             constexpr uint32_t kStageD = kStage >> 4, kAD = kABytes >> 4, kBOffD = (U * kABytes) >> 4,
                                kBTileD = kBTile >> 4;
@@ -315,14 +318,14 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
             int64_t tile = blockIdx.x;
             for (int i = 0; tile < a.n_tiles && ok; tile += stride, ++i) {
                 const int b = i & 1;
-                if (!mbar_wait(&tempty[b], ((i >> 1) & 1) ^ 1, abort)) break;
+                if (!mbar_wait_warp(&tempty[b], ((i >> 1) & 1) ^ 1, abort)) break;
                 tc_fence_after();
                 const uint32_t d = tmem + b * BN;
                 const int n_units = tile_units<PACK>(a, tile).n;
                 uint32_t acc = 0;
                 int c = 0;
                 for (int u0 = 0; u0 < n_units; u0 += U) {
-                    if (!mbar_wait(&full[stage], phase, abort)) {
+                    if (!mbar_wait_warp(&full[stage], phase, abort)) {
                         ok = false;
                         break;
                     }
@@ -340,13 +343,13 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                         for (int h = 0; h < 4; ++h) {  // 32 bytes of K per MMA
                             if (h >= nk) break;
                             if (EBYTES == 2)
-                                mma_f16(d, ad + u * kAD + 2 * h, bd + u * kBTileD + 2 * h, idesc, acc);
+                                mma_f16_warp(d, ad + u * kAD + 2 * h, bd + u * kBTileD + 2 * h, idesc, acc);
                             else
-                                mma_f8(d, ad + u * kAD + 2 * h, bd + u * kBTileD + 2 * h, idesc, acc);
+                                mma_f8_warp(d, ad + u * kAD + 2 * h, bd + u * kBTileD + 2 * h, idesc, acc);
                             acc = 1;
                         }
                     }
-                    mma_commit(&empty[stage]);
+                    mma_commit_warp(&empty[stage]);
                     if (++stage == (uint32_t)S) {
                         stage = 0;
                         phase ^= 1;
@@ -354,12 +357,12 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                 }
                 if (!ok) break;
                 if (acc)
-                    mma_commit(&tfull[b]);
+                    mma_commit_warp(&tfull[b]);
                 else
-                    mbar_arrive(&tfull[b]);
+                    mbar_arrive_warp(&tfull[b]);
             }
             // all issued MMAs complete before TMEM is released
-            mma_commit(fin);
+            mma_commit_warp(fin);
             const long long t0 = clock64();
             while (!mbar_try_wait_sleep(fin, 0, kSuspendNs) && clock64() - t0 < kWaitCycles) {
             }

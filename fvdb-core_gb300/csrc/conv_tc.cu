@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
         return (a.tile_mask[(r_begin / kTileM) + t] & gbits) != 0;
     };
 
-    int steps = 0;  // active stages: the gather warps run the same loop as the MMA thread
+    int steps = 0;  // active stages: the gather warps run the same loop as the MMA warp
     if (warp < kWgGatherWarps) {
         // Lane -> (16-byte chunk jj of a 128-byte MN atom row, K-rows rsub + 4q of this warp's
         // 16): one warp instruction moves four whole 128-byte atom rows of an operand.  Atom a of
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
                 }
             }
             // cp.async and st.shared are generic-proxy writes: each warp fences its own copies to
-            // the tensor core (async proxy), one stage late, so the MMA thread never fences
+            // the tensor core (async proxy), one stage late, so the MMA warp never fences
             cp_async_commit();
             ++it;
             if (++stage == (uint32_t)S) {
@@ -269,27 +269,28 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_wgrad_kernel(WgArgs a) {
                 mbar_arrive(&full[pstage]);
                 if (++pstage == (uint32_t)S) pstage = 0;
             }
-    } else if (warp == kWgMmaWarp && lane == 0) {
+    } else if (warp == kWgMmaWarp) {
+        // the whole warp runs the issue loop (warp-uniform); one elected lane issues each tcgen05 op
         constexpr uint32_t idesc = idesc_m128(BN, 1, 1) | (1u << 15) | (1u << 16);  // bf16, A and B MN-major
         int it = 0;
         for (int64_t t = 0; t < n_tiles; ++t) {
             if (!tile_active(t)) continue;
             const int stage = it % S;
-            if (!mbar_wait(&full[stage], (it / S) & 1, abort)) break;
+            if (!mbar_wait_warp(&full[stage], (it / S) & 1, abort)) break;
             tc_fence_after();
             const uint32_t As = smem_u32(smem + stage * kStage), Bs = As + kBOff;
 #pragma unroll
             for (int q = 0; q < kTileM / 16; ++q)  // 16 rows of K per MMA = two 8-row groups
-                mma_f16(tmem, desc_sw128_mn(As + q * 2048), desc_sw128_mn(Bs + q * 2048), idesc,
-                        (it > 0 || q > 0) ? 1u : 0u);
-            mma_commit(&empty[stage]);
+                mma_f16_warp(tmem, desc_sw128_mn(As + q * 2048), desc_sw128_mn(Bs + q * 2048), idesc,
+                             (it > 0 || q > 0) ? 1u : 0u);
+            mma_commit_warp(&empty[stage]);
             ++it;
         }
         // it == 0: nothing accumulated -- the epilogue writes zeros
         if (it > 0)
-            mma_commit(accum);
+            mma_commit_warp(accum);
         else
-            mbar_arrive(accum);
+            mbar_arrive_warp(accum);
     }
     if (warp < 4) {
         const bool have = __all_sync(0xffffffffu, mbar_wait(accum, 0, abort) && !*abort);

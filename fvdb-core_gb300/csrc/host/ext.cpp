@@ -14,6 +14,7 @@
 #include <c10/cuda/CUDAGuard.h>
 #include <torch/extension.h>
 
+#include <map>
 #include <optional>
 #include <string>
 #include <vector>
@@ -44,12 +45,11 @@ Tensor workspace(size_t bytes, const torch::Device &dev) {
     return torch::empty({(int64_t)std::max<size_t>(bytes, 256)}, torch::dtype(torch::kUInt8).device(dev));
 }
 
-// Pinned host staging for the small device-to-host reads of grid builds (per device, grown on
-// demand): one async copy and one stream sync instead of a torch gather + copy.
+// Pinned host staging for the small device-to-host reads of grid builds (per host thread and
+// device, grown on demand): one async copy and one stream sync instead of a torch gather +
+// copy.  Per thread, so grid builds of concurrent serving slots never share it.
 int64_t *pinned_meta(int dev, size_t count) {
-    static std::mutex mu;
-    static std::vector<std::pair<int64_t *, size_t>> bufs(64, {nullptr, 0});
-    std::lock_guard<std::mutex> lock(mu);
+    thread_local std::vector<std::pair<int64_t *, size_t>> bufs(64, {nullptr, 0});
     auto &b = bufs.at(dev);
     if (b.second < count) {
         if (b.first) cudaFreeHost(b.first);
@@ -354,6 +354,10 @@ struct PackInfo {
     std::optional<bool> gs_use_me;
     int64_t split_mask_num = 1;
     bool training_built = false;
+    // tile plans of the forward (0) / transposed (1) map per feature row size in bytes, and how
+    // often each was asked for
+    std::map<std::pair<int, int32_t>, Tensor> plans;
+    std::map<std::pair<int, int32_t>, int> plan_requests;
 };
 using PackPtr = std::shared_ptr<PackInfo>;
 
@@ -439,6 +443,49 @@ std::optional<Tensor> pack_tile_mask(PackPtr p, bool transposed) {
     }
     if (!p->tile_mask_t) p->tile_mask_t = tile_masks_of(pack_kmap_t(p), p->src->N, p->K);
     return p->tile_mask_t;
+}
+
+// Whether a contraction may run over a tile plan (fvgb_conv_fwd_tc_planned) instead of over the
+// map directly (fvgb_conv_fwd_tc_bias).  Measured on GB300 (1.08M surface voxels, 3x3x3): the
+// planned kernel is faster for rows shorter than 128 bytes (32->64 BF16: 0.31 vs 0.37 ms) and
+// slower for 128-byte rows (64->64 BF16: 0.73 vs 0.6 ms), where assembling the A operand in
+// tensor memory costs more than the gathers it saves; so plans serve short rows only.
+bool use_plan(int32_t dtype, int64_t K, int64_t cin, int64_t cout, int64_t elem) {
+    return cin * elem < 128 && fvgb_tc_plan_supported(dtype, (int32_t)K, (int32_t)cin, (int32_t)cout) == FVGB_OK;
+}
+
+std::optional<Tensor> pack_plan(PackPtr p, bool transposed, int32_t row_bytes);
+
+// The plan of a map and row size once it is worth building: building one costs about 0.7x a
+// contraction over the map (0.26 ms for 1.08M rows x 27), and a contraction over it saves about
+// 0.2x, so the first contraction on a (map, row size) runs unplanned and the plan is built at the
+// second and reused by every later one (layers that share a kernel map, training iterations on a
+// cached map).
+std::optional<Tensor> pack_plan_if_reused(PackPtr p, bool transposed, int32_t row_bytes) {
+    const auto key = std::make_pair(transposed ? 1 : 0, row_bytes);
+    if (p->plans.count(key)) return p->plans[key];
+    if (++p->plan_requests[key] < 2) return std::nullopt;
+    return pack_plan(p, transposed, row_bytes);
+}
+
+// Tile plan (staging schedule of the planned tensor-core kernel) of the forward map
+// (transposed=false) or of the transposed map, for feature rows of row_bytes bytes; built once
+// per pack and row size.  nullopt where the planned kernel does not take the shape.
+std::optional<Tensor> pack_plan(PackPtr p, bool transposed, int32_t row_bytes) {
+    if (p->K > 32) return std::nullopt;
+    const auto key = std::make_pair(transposed ? 1 : 0, row_bytes);
+    auto it = p->plans.find(key);
+    if (it != p->plans.end()) return it->second;
+    const Tensor &m = transposed ? pack_kmap_t(p) : pack_kmap(p);
+    const int64_t n = transposed ? p->src->N : p->tgt->N;
+    size_t bytes = 0;
+    if (fvgb_tc_plan_bytes(n, p->K, row_bytes, &bytes) != FVGB_OK) return std::nullopt;
+    Tensor plan = torch::empty({(int64_t)std::max<size_t>(bytes, 16)}, m.options().dtype(torch::kUInt8));
+    check_status(fvgb_tc_plan_build(m.data_ptr<int32_t>(), n, p->K, row_bytes, plan.data_ptr(), (size_t)plan.numel(),
+                                    cur_stream()),
+                 "tile plan build");
+    p->plans[key] = plan;
+    return plan;
 }
 
 void pack_build_gather_scatter(PackPtr p, bool use_me) {
@@ -535,15 +582,21 @@ void pack_build_implicit_gemm(PackPtr p, bool sorted, int64_t split, bool traini
 // ------------------------------------------------------------------------------------------
 // Contractions.  W is viewed as [K, Cin, Cout] (any strides).
 
-// Device flag that the tensor-core kernels raise when a bounded wait gives up (per device).
+// Device flag that the tensor-core kernels raise when a bounded wait gives up: one per (device,
+// CUDA stream), so a timeout is reported to the work of the stream it happened on (serving slots
+// run on streams of their own).
 Tensor &device_error_flag(const torch::Device &dev) {
-    static std::vector<Tensor> flags(64);
-    Tensor &f = flags.at(dev.index());
+    static std::mutex mu;
+    static std::map<std::pair<int, uintptr_t>, Tensor> flags;
+    const uintptr_t stream = reinterpret_cast<uintptr_t>(at::cuda::getCurrentCUDAStream(dev.index()).stream());
+    std::lock_guard<std::mutex> lock(mu);
+    Tensor &f = flags[{(int)dev.index(), stream}];
     if (!f.defined()) f = torch::zeros({1}, torch::dtype(torch::kInt32).device(dev));
     return f;
 }
 
-// Raises if a tensor-core kernel on `dev` reported a timeout (synchronises the device).
+// Raises if a tensor-core kernel on the current stream of `dev` reported a timeout
+// (synchronises with that stream's work).
 void check_device_errors(const torch::Device &dev) {
     Tensor &f = device_error_flag(dev);
     const int v = f.item<int>();
@@ -563,9 +616,11 @@ bool use_tensor_cores(const Tensor &x, int64_t cin, int64_t cout) {
 
 // y[m] = sum_k x[map[m,k]] W[k]   for the first n_out rows of map
 // bias (optional, [cout]): added in the tensor-core epilogue, else after the contraction.
+// pack / map_t (optional): the pack info that owns `map` and whether `map` is its transposed map;
+// with them, shapes the planned kernel takes run over the pack's cached tile plan.
 Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &Wkio, bool transpose_w,
                    const std::optional<Tensor> &tile_mask = std::nullopt,
-                   const std::optional<Tensor> &bias = std::nullopt) {
+                   const std::optional<Tensor> &bias = std::nullopt, PackPtr pack = nullptr, bool map_t = false) {
     c10::cuda::CUDAGuard guard(x.device());
     const int64_t K = map.size(1);
     const int64_t cin = transpose_w ? Wkio.size(2) : Wkio.size(1);
@@ -587,6 +642,17 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
         const uint32_t *tm = tile_mask ? reinterpret_cast<const uint32_t *>(tile_mask->data_ptr<int32_t>()) : nullptr;
         Tensor b32;
         if (bias) b32 = bias->to(torch::kFloat32).contiguous();
+        std::optional<Tensor> plan;
+        if (pack && use_plan(FVGB_BF16, K, cin, cout, 2)) plan = pack_plan_if_reused(pack, map_t, (int32_t)(cin * 2));
+        if (plan) {
+            check_status(fvgb_conv_fwd_tc_planned(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
+                                                  plan->data_ptr(), n_out, (int32_t)K, packed.data_ptr(),
+                                                  (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
+                                                  bias ? b32.data_ptr<float>() : nullptr,
+                                                  device_error_flag(x.device()).data_ptr<int32_t>(), s),
+                         "sparse conv forward (tensor cores)");
+            return y;
+        }
         check_status(fvgb_conv_fwd_tc_bias(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
                                            map.data_ptr<int32_t>(), n_out, (int32_t)K, tm, packed.data_ptr(),
                                            (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
@@ -694,10 +760,10 @@ std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr
     }
     Tensor y;
     if (!transposed)
-        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false), bias)
+        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false), bias, p, false)
                       : torch::empty({0, cout}, x.options());
     else
-        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true), bias)
+        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true), bias, p, true)
                       : torch::empty({0, cout}, x.options());
     return {y, Wkio};
 }
@@ -710,10 +776,12 @@ std::vector<Tensor> conv_backward(const Tensor &dy_in, const Tensor &x, const Te
     Tensor dx, dW;
     if (!transposed) {
         // dgrad: dx[i] = sum_k dy[mapT[i,k]] W[k]^T ;  wgrad: dW[k] = sum_m x[map[m,k]]^T dy[m]
-        if (need_dx) dx = gather_gemm(dy, pack_kmap_t(p), p->src->N, Wkio, true, pack_tile_mask(p, true));
+        if (need_dx)
+            dx = gather_gemm(dy, pack_kmap_t(p), p->src->N, Wkio, true, pack_tile_mask(p, true), std::nullopt, p, true);
         if (need_dw) dW = gather_wgrad(x, pack_kmap(p), p->tgt->N, dy, K, pack_tile_mask(p, false));
     } else {
-        if (need_dx) dx = gather_gemm(dy, pack_kmap(p), p->tgt->N, Wkio, true, pack_tile_mask(p, false));
+        if (need_dx)
+            dx = gather_gemm(dy, pack_kmap(p), p->tgt->N, Wkio, true, pack_tile_mask(p, false), std::nullopt, p, false);
         if (need_dw) dW = gather_wgrad(x, pack_kmap_t(p), p->src->N, dy, K, pack_tile_mask(p, true));
     }
     if (need_dw) {
@@ -766,6 +834,16 @@ std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, Pac
     const Tensor &map = transposed ? pack_kmap_t(p) : pack_kmap(p);
     auto tm = pack_tile_mask(p, transposed);
     Tensor sw = s_w.contiguous();
+    std::optional<Tensor> plan;
+    if (use_plan(FVGB_E4M3, K, cin, cout, 1)) plan = pack_plan_if_reused(p, transposed, (int32_t)cin);
+    if (plan) {
+        check_status(fvgb_conv_fwd_tc_planned(FVGB_E4M3, x8.data_ptr(), x8.size(0), (int32_t)cin, cin, plan->data_ptr(),
+                                              n_rows, (int32_t)K, packed.data_ptr(), (int32_t)cout, y.data_ptr(),
+                                              y.stride(0), sw.data_ptr<float>(), nullptr,
+                                              device_error_flag(x.device()).data_ptr<int32_t>(), s),
+                     "sparse conv forward (fp8 tensor cores)");
+        return {y, s_x, s_w};
+    }
     check_status(fvgb_conv_fwd_tc(FVGB_E4M3, x8.data_ptr(), x8.size(0), (int32_t)cin, cin, map.data_ptr<int32_t>(), n_rows,
                                   (int32_t)K, tm ? reinterpret_cast<const uint32_t *>(tm->data_ptr<int32_t>()) : nullptr,
                                   packed.data_ptr(), (int32_t)cout, y.data_ptr(), y.stride(0), sw.data_ptr<float>(),
@@ -786,10 +864,10 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
 
     py::class_<GridImpl, GridPtr>(m, "GridImpl")
         .def_static("from_ijk", &grid_from_ijk, py::arg("ijk"), py::arg("joffsets"), py::arg("voxel_sizes"),
-                    py::arg("origins"))
+                    py::arg("origins"), py::call_guard<py::gil_scoped_release>())
         .def_static("from_points", &grid_from_points, py::arg("points"), py::arg("joffsets"),
-                    py::arg("voxel_sizes"), py::arg("origins"))
-        .def("conv_grid", &grid_conv_grid)
+                    py::arg("voxel_sizes"), py::arg("origins"), py::call_guard<py::gil_scoped_release>())
+        .def("conv_grid", &grid_conv_grid, py::call_guard<py::gil_scoped_release>())
         .def_property_readonly("grid_count", [](const GridImpl &g) { return g.B; })
         .def_property_readonly("total_voxels", [](const GridImpl &g) { return g.N; })
         .def_property_readonly("total_leaf_nodes", [](const GridImpl &g) { return g.L; })
@@ -813,6 +891,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def("kmap_t", [](PackPtr p) { return pack_kmap_t(p); })
         .def("tile_mask", [](PackPtr p, bool transposed) { return pack_tile_mask(p, transposed); },
              py::arg("transposed") = false)
+        .def("tile_plan", [](PackPtr p, bool transposed, int32_t row_bytes) { return pack_plan(p, transposed, row_bytes); },
+             py::arg("transposed"), py::arg("row_bytes"))
         .def("build_gather_scatter", &pack_build_gather_scatter)
         .def("build_implicit_gemm", &pack_build_implicit_gemm)
         .def_property_readonly("kernel_size", [](const PackInfo &p) { return py::make_tuple(p.ks.v[0], p.ks.v[1], p.ks.v[2]); })
@@ -834,9 +914,12 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def_property_readonly("use_me", [](const PackInfo &p) { return p.use_me; })
         .def_property_readonly("use_tf32", [](const PackInfo &p) { return p.use_tf32; });
 
+    // the GIL is released while the native calls run (their grid builds wait for a count read),
+    // so host threads of concurrent serving slots do not serialise on it
     m.def("conv_forward", &conv_forward, py::arg("features"), py::arg("weights"), py::arg("pack"),
-          py::arg("transposed"), py::arg("bias") = py::none());
-    m.def("conv_forward_fp8", &conv_forward_fp8);
-    m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); });
-    m.def("conv_backward", &conv_backward);
+          py::arg("transposed"), py::arg("bias") = py::none(), py::call_guard<py::gil_scoped_release>());
+    m.def("conv_forward_fp8", &conv_forward_fp8, py::call_guard<py::gil_scoped_release>());
+    m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); },
+          py::call_guard<py::gil_scoped_release>());
+    m.def("conv_backward", &conv_backward, py::call_guard<py::gil_scoped_release>());
 }

@@ -255,20 +255,31 @@ class ConvStack:
 
 
 class GPUExecutor(Executor):
-    """Packs a batch into one jagged GridBatch on the slot's CUDA stream and runs the stack."""
+    """Packs a batch into one jagged GridBatch and runs the stack on the slot's CUDA stream.
+
+    Each slot has a host worker thread of its own: launch() only hands the batch to it, so the
+    scheduler never waits for a grid build's count read (the one host synchronisation of a
+    build) and keeps admitting requests while batches are being built and run.  The native
+    calls release the GIL while they wait.  Each slot's kernels report bounded-wait timeouts
+    through the error flag of the slot's stream, so a failure is charged to its own batch."""
 
     def __init__(self, model: ConvStack, device, slots: int = 2):
+        import concurrent.futures
+
         self.model = model
         self.device = torch.device(device)
-        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max(slots, 1))]
+        n = max(slots, 1)
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(n)]
+        self.workers = [concurrent.futures.ThreadPoolExecutor(max_workers=1, thread_name_prefix=f"fvdb-slot{i}")
+                        for i in range(n)]
 
     def footprint(self, req: Request) -> int:
         return req.n_voxels * self.model.bytes_per_voxel() + (1 << 20)
 
-    def launch(self, batch: list[Request], slot: int):
+    def _run(self, batch: list[Request], slot: int):
         fvdb = self.model.fvdb
         stream = self.streams[slot % len(self.streams)]
-        with torch.cuda.stream(stream):
+        with torch.cuda.device(self.device), torch.cuda.stream(stream):
             ijk = torch.cat([r.ijk for r in batch]).to(self.device, non_blocking=True)
             feats = torch.cat([r.features for r in batch]).to(self.device, non_blocking=True)
             offs = torch.tensor([0] + [r.n_voxels for r in batch], dtype=torch.int64).cumsum(0)
@@ -285,19 +296,31 @@ class GPUExecutor(Executor):
             out_ijk.copy_(grid.ijk.jdata, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
-        return (ev, batch, out, out_ijk, grid.joffsets.cpu())
+        # the grid's voxel offsets were read to the host by its build: no device read here
+        return ev, out, out_ijk, grid._impl.joffsets_host.tolist()
+
+    def launch(self, batch: list[Request], slot: int):
+        return (self.workers[slot % len(self.workers)].submit(self._run, batch, slot), batch, slot)
 
     def poll(self, handle) -> bool:
-        return handle[0].query()
+        fut = handle[0]
+        if not fut.done():
+            return False
+        return fut.exception() is not None or fut.result()[0].query()
 
     def finish(self, handle) -> None:
-        ev, batch, out, out_ijk, offs = handle
+        fut, batch, slot = handle
+        ev, out, out_ijk, o = fut.result()  # re-raises a failure of the build or the launch
         ev.synchronize()
-        self.model.fvdb._lib.load().check_device_errors(self.device)
-        o = offs.tolist()
+        with torch.cuda.device(self.device), torch.cuda.stream(self.streams[slot % len(self.streams)]):
+            self.model.fvdb._lib.load().check_device_errors(self.device)
         for b, r in enumerate(batch):
             r.output = out[o[b] : o[b + 1]]
             r.out_ijk = out_ijk[o[b] : o[b + 1]]
+
+    def close(self) -> None:
+        for w in self.workers:
+            w.shutdown(wait=True)
 
 
 def run_alone(model: ConvStack, req: Request, device) -> tuple[torch.Tensor, torch.Tensor]:

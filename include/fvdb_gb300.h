@@ -326,6 +326,38 @@ int fvgb_conv_fwd_tc_bias(int32_t dtype, const void *x, int64_t n_x, int32_t c_i
                           fvgb_stream_t stream);
 
 /*
+ * Tile plan of a kernel map for the planned tensor-core convolution: for every 128-row tile of
+ * `map` ([ceil(n_rows/128)*128, K] int32, -1 = absent, K <= 32) the distinct source rows it
+ * reads (split into phases that fit the kernel's staging buffer, which depends on row_bytes =
+ * c_in * element size) and each entry's 16-bit index into its phase's row list.  Built once per
+ * kernel map and feature row size; fvgb_tc_plan_bytes gives its size.  No reference counterpart
+ * of the plan itself: it is the staging schedule of the kernel that replaces
+ * dispatchSparseConvolutionImplicitGEMM[Sorted]<kCUDA> (see fvgb_conv_fwd_tc).
+ */
+int fvgb_tc_plan_bytes(int64_t n_rows, int32_t K, int32_t row_bytes, size_t *bytes);
+int fvgb_tc_plan_build(const int32_t *map, int64_t n_rows, int32_t K, int32_t row_bytes, void *plan,
+                       size_t plan_bytes, fvgb_stream_t stream);
+
+/* FVGB_OK when fvgb_conv_fwd_tc_planned takes (dtype, K, c_in, c_out): K <= 32, c_out <= 128,
+ * c_in * element size a multiple of 32 bytes up to 256 that tiles 128 bytes when shorter. */
+int fvgb_tc_plan_supported(int32_t dtype, int32_t K, int32_t c_in, int32_t c_out);
+
+/*
+ * fvgb_conv_fwd_tc_bias over a tile plan of the same map (fvgb_tc_plan_build with
+ * row_bytes = c_in * element size): each tile's distinct input rows are staged in shared memory
+ * once and the gathered A operand is assembled in tensor memory, so no map entry is gathered
+ * from L2 on its own.  Same arguments, weight image, result and error flag as
+ * fvgb_conv_fwd_tc_bias (the map and tile masks are read from the plan).  Replaces
+ * dispatchSparseConvolutionImplicitGEMM[Sorted]<kCUDA>
+ * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionImplicitGEMM.cu:2754-3826,
+ * SparseConvolutionImplicitGEMMSorted.cu:3101-4641).
+ */
+int fvgb_conv_fwd_tc_planned(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                             const void *plan, int64_t n_out, int32_t K, const void *packed_w, int32_t c_out,
+                             void *y, int64_t ldy, const float *out_scale, const float *bias, int32_t *err_dev,
+                             fvgb_stream_t stream);
+
+/*
  * Tensor-core weight gradient, BF16 operands:  dw[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co]
  * (FP32, [K, c_in, c_out] contiguous).  c_in in {32, 64, 128} (128/c_in offsets share one
  * M=128 MMA), c_out in {64, 128, 256}; rows of x and dy 16-byte aligned.  Per-CTA FP32
