@@ -852,6 +852,160 @@ std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, Pac
     return {y, s_x, s_w};
 }
 
+// ------------------------------------------------------------------------------------------
+// Pooling / nearest upsampling between grids (GridBatch::max_pool / avg_pool / subdivide,
+// src/fvdb/GridBatch.cpp:241-345) and the grids they default to.
+
+// coarsened_grid(f): floor(ijk / f) per axis (GridBatch::coarsened_grid, BuildCoarseGridFromFine.cu:22-82),
+// the coarse path of conv_grid with kernel == stride == f.
+GridPtr grid_coarsened(const GridPtr &g, const std::vector<int64_t> &f) {
+    Vec3 v = to_vec3(f, "coarsening_factor");
+    for (int a = 0; a < 3; ++a) TORCH_CHECK_VALUE(v.v[a] > 0, "coarsening_factor must be positive");
+    std::vector<int64_t> ff = {v.v[0], v.v[1], v.v[2]};
+    GridPtr c = grid_conv_grid(g, ff, ff);
+    // coarse transform (GridBatchImpl.cu:645-655): size f*w, origin (f-1)*w*0.5 + o
+    Tensor fv = torch::tensor({(double)v.v[0], (double)v.v[1], (double)v.v[2]}, torch::kFloat64);
+    c->voxel_sizes = fv * g->voxel_sizes;
+    c->origins = (fv - 1.0) * g->voxel_sizes * 0.5 + g->origins;
+    return c;
+}
+
+// subdivided_grid(f, mask): every (masked) voxel c gives c*f + (i,j,k) (GridBatch::subdivided_grid,
+// BuildFineGridFromCoarse.cu:66-226).
+GridPtr grid_subdivided(const GridPtr &g, const std::vector<int64_t> &f, const std::optional<Tensor> &mask) {
+    c10::cuda::CUDAGuard guard(g->device());
+    Vec3 v = to_vec3(f, "subdiv_factor");
+    for (int a = 0; a < 3; ++a) TORCH_CHECK_VALUE(v.v[a] > 0, "subdiv_factor must be positive");
+    const int64_t V = (int64_t)v.v[0] * v.v[1] * v.v[2];
+    TORCH_CHECK_VALUE(V <= 512, "subdiv_factor volume must be at most 512");
+    auto dev = g->device();
+    Tensor m;
+    if (mask) {
+        TORCH_CHECK_VALUE(mask->dim() == 1 && mask->size(0) == g->N, "mask must have one entry per voxel");
+        m = mask->to(dev, torch::kUInt8).contiguous();
+    }
+    const int64_t n = g->N * V;
+    auto i32 = torch::dtype(torch::kInt32).device(dev);
+    Tensor cand = torch::empty({std::max<int64_t>(n, 1), 3}, i32);
+    Tensor valid = torch::empty({std::max<int64_t>(n, 1)}, torch::dtype(torch::kUInt8).device(dev));
+    FvgbGrid gv = g->view();
+    auto s = cur_stream();
+    check_status(fvgb_subdivide_candidates(&gv, v.v, mask ? m.data_ptr<uint8_t>() : nullptr, cand.data_ptr<int32_t>(),
+                                           valid.data_ptr<uint8_t>(), s),
+                 "subdivided_grid (candidates)");
+    Tensor out = torch::empty({std::max<int64_t>(n, 1), 3}, i32);
+    Tensor joff = torch::empty({g->B + 1}, torch::dtype(torch::kInt64).device(dev));
+    size_t sb = 0;
+    check_status(fvgb_scan_workspace(n, &sb), "subdivided_grid (workspace)");
+    Tensor ws = workspace(sb, dev);
+    check_status(fvgb_compact_ijk(cand.data_ptr<int32_t>(), valid.data_ptr<uint8_t>(), g->joffsets.data_ptr<int64_t>(),
+                                  (int32_t)g->B, V, n, out.data_ptr<int32_t>(), joff.data_ptr<int64_t>(), ws.data_ptr(),
+                                  ws.numel(), s),
+                 "subdivided_grid (compact)");
+    const int64_t mcount = n > 0 ? joff[g->B].item<int64_t>() : 0;
+    // fine transform (GridBatchImpl.cu:633-643): size w/f, origin o - (f-1)*(w/f)*0.5
+    Tensor fv = torch::tensor({(double)v.v[0], (double)v.v[1], (double)v.v[2]}, torch::kFloat64);
+    Tensor vs = g->voxel_sizes / fv;
+    Tensor org = g->origins - (fv - 1.0) * (g->voxel_sizes / fv) * 0.5;
+    if (g->N == 0) return build_grid(out.narrow(0, 0, 0), joff, vs, org);
+    int32_t lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = g->box_lo[a] * v.v[a];
+        hi[a] = g->box_hi[a] * v.v[a] + v.v[a] - 1;
+    }
+    return build_grid(out.narrow(0, 0, mcount), joff, vs, org, lo, hi);
+}
+
+Tensor flat2d(const Tensor &t) { return t.reshape({t.size(0), -1}).contiguous(); }
+
+// y [coarse N, C] = max / average pooling of x [fine N, *] (mode FVGB_POOL_MAX / FVGB_POOL_AVG)
+Tensor pool_forward(int32_t mode, const GridPtr &fine, const GridPtr &coarse, const std::vector<int64_t> &pool,
+                    const std::vector<int64_t> &stride, const Tensor &x) {
+    c10::cuda::CUDAGuard guard(fine->device());
+    TORCH_CHECK_VALUE(x.dim() > 1, "fine_data must have more than one dimension. i.e. have shape (num_voxels, *)");
+    TORCH_CHECK_VALUE(x.size(0) == fine->N, "fine_data must have the same number of voxels as fine_grid");
+    TORCH_CHECK(fine->device() == coarse->device(), "coarse_grid and fine_grid must be on the same device");
+    Vec3 p = to_vec3(pool, "pool_factor"), st = to_vec3(stride, "stride");
+    for (int a = 0; a < 3; ++a) {
+        TORCH_CHECK_VALUE(p.v[a] > 0, "pooling_factor must be greater than 0");
+        TORCH_CHECK_VALUE(st.v[a] >= 0, "stride must be greater than or equal to 0");
+        if (st.v[a] == 0) st.v[a] = p.v[a];
+    }
+    Tensor xf = flat2d(x);
+    const int64_t C = xf.size(1);
+    std::vector<int64_t> shape = x.sizes().vec();
+    shape[0] = coarse->N;
+    Tensor y = torch::empty({coarse->N, std::max<int64_t>(C, 1)}, x.options());
+    if (C > 0 && coarse->N > 0) {
+        FvgbGrid fv = fine->view(), cv = coarse->view();
+        check_status(fvgb_pool_forward(mode, fvgb_dtype(x), &fv, &cv, p.v, st.v, fine->N ? xf.data_ptr() : nullptr,
+                                       C, (int32_t)C, y.data_ptr(), C, cur_stream()),
+                     mode == FVGB_POOL_MAX ? "max_pool" : "avg_pool");
+    }
+    return y.narrow(1, 0, C).reshape(shape);
+}
+
+Tensor pool_backward(int32_t mode, const GridPtr &fine, const GridPtr &coarse, const std::vector<int64_t> &pool,
+                     const std::vector<int64_t> &stride, const Tensor &x, const Tensor &dy) {
+    c10::cuda::CUDAGuard guard(fine->device());
+    Vec3 p = to_vec3(pool, "pool_factor"), st = to_vec3(stride, "stride");
+    for (int a = 0; a < 3; ++a)
+        if (st.v[a] == 0) st.v[a] = p.v[a];
+    Tensor xf = flat2d(x), df = flat2d(dy.to(x.scalar_type()));
+    const int64_t C = xf.size(1);
+    FvgbGrid fv = fine->view(), cv = coarse->view();
+    auto s = cur_stream();
+    if (C == 0 || fine->N == 0) return torch::zeros_like(x);
+    if (mode == FVGB_POOL_MAX) {
+        const auto acc = x.scalar_type() == torch::kFloat64 ? torch::kFloat64 : torch::kFloat32;
+        Tensor dacc = torch::zeros({fine->N, C}, x.options().dtype(acc));
+        check_status(fvgb_maxpool_backward(fvgb_dtype(x), &fv, &cv, p.v, st.v, xf.data_ptr(), C, (int32_t)C,
+                                           coarse->N ? df.data_ptr() : nullptr, C, dacc.data_ptr(), s),
+                     "max_pool backward");
+        return dacc.to(x.scalar_type()).reshape(x.sizes());
+    }
+    Tensor dx = torch::empty({fine->N, C}, x.options());
+    check_status(fvgb_avgpool_backward(fvgb_dtype(x), &fv, &cv, p.v, st.v, (int32_t)C, coarse->N ? df.data_ptr() : nullptr,
+                                       C, dx.data_ptr(), C, s),
+                 "avg_pool backward");
+    return dx.reshape(x.sizes());
+}
+
+// y [fine N, *] = nearest upsampling of x [coarse N, *]
+Tensor upsample_forward(const GridPtr &coarse, const GridPtr &fine, const std::vector<int64_t> &factor, const Tensor &x) {
+    c10::cuda::CUDAGuard guard(fine->device());
+    TORCH_CHECK_VALUE(x.dim() > 1 && x.size(0) == coarse->N, "data must have shape (num_voxels, *) of the coarse grid");
+    Vec3 f = to_vec3(factor, "subdiv_factor");
+    Tensor xf = flat2d(x);
+    const int64_t C = xf.size(1);
+    std::vector<int64_t> shape = x.sizes().vec();
+    shape[0] = fine->N;
+    Tensor y = torch::empty({fine->N, std::max<int64_t>(C, 1)}, x.options());
+    if (C > 0 && fine->N > 0) {
+        FvgbGrid fv = fine->view(), cv = coarse->view();
+        check_status(fvgb_upsample_forward(fvgb_dtype(x), &cv, &fv, f.v, coarse->N ? xf.data_ptr() : nullptr, C,
+                                           (int32_t)C, y.data_ptr(), C, cur_stream()),
+                     "subdivide");
+    }
+    return y.narrow(1, 0, C).reshape(shape);
+}
+
+Tensor upsample_backward(const GridPtr &coarse, const GridPtr &fine, const std::vector<int64_t> &factor, const Tensor &dy,
+                         const Tensor &x) {
+    c10::cuda::CUDAGuard guard(fine->device());
+    Vec3 f = to_vec3(factor, "subdiv_factor");
+    Tensor df = flat2d(dy.to(x.scalar_type()));
+    const int64_t C = df.size(1);
+    Tensor dx = torch::empty({coarse->N, std::max<int64_t>(C, 1)}, x.options());
+    if (C > 0 && coarse->N > 0) {
+        FvgbGrid fv = fine->view(), cv = coarse->view();
+        check_status(fvgb_upsample_backward(fvgb_dtype(x), &cv, &fv, f.v, fine->N ? df.data_ptr() : nullptr, C,
+                                            (int32_t)C, dx.data_ptr(), C, cur_stream()),
+                     "subdivide backward");
+    }
+    return dx.narrow(1, 0, C).reshape(x.sizes());
+}
+
 std::optional<Tensor> opt(const std::optional<Tensor> &t) { return t; }
 
 }  // namespace fvgbh
@@ -868,6 +1022,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def_static("from_points", &grid_from_points, py::arg("points"), py::arg("joffsets"),
                     py::arg("voxel_sizes"), py::arg("origins"), py::call_guard<py::gil_scoped_release>())
         .def("conv_grid", &grid_conv_grid, py::call_guard<py::gil_scoped_release>())
+        .def("coarsened_grid", &grid_coarsened, py::call_guard<py::gil_scoped_release>())
+        .def("subdivided_grid", &grid_subdivided, py::arg("subdiv_factor"), py::arg("mask") = py::none())
         .def_property_readonly("grid_count", [](const GridImpl &g) { return g.B; })
         .def_property_readonly("total_voxels", [](const GridImpl &g) { return g.N; })
         .def_property_readonly("total_leaf_nodes", [](const GridImpl &g) { return g.L; })
@@ -922,4 +1078,10 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); },
           py::call_guard<py::gil_scoped_release>());
     m.def("conv_backward", &conv_backward, py::call_guard<py::gil_scoped_release>());
+    m.def("pool_forward", &pool_forward);
+    m.def("pool_backward", &pool_backward);
+    m.def("upsample_forward", &upsample_forward);
+    m.def("upsample_backward", &upsample_backward);
+    m.attr("POOL_MAX") = (int)FVGB_POOL_MAX;
+    m.attr("POOL_AVG") = (int)FVGB_POOL_AVG;
 }

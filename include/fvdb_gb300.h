@@ -393,6 +393,45 @@ int fvgb_quantize_e4m3(int32_t dtype, const void *x, int64_t n, int32_t c, int64
  */
 int fvgb_selftest_wait_timeout(int32_t *err_dev, int64_t budget_cycles, int32_t arrive, fvgb_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Pooling and nearest upsampling between a fine and a coarse grid of the same batch.
+ * Features [n, C] rows in grid index order (ld = row stride in elements), dtype FVGB_F32 /
+ * FVGB_F64 / FVGB_F16 / FVGB_BF16.  Window / factor volume at most 512.
+ * ------------------------------------------------------------------------------------------ */
+enum { FVGB_POOL_MAX = 0, FVGB_POOL_AVG = 1 };
+
+/* y[c] = max (or average) of fine voxels c*stride + (i,j,k), i<pool[0], j<pool[1], k<pool[2]
+ * (max of an empty window = -inf; average = window sum * 1/(pool volume), rounded as the
+ * reference).  Replaces DownsampleGridMaxPool / DownsampleGridAvgPool
+ * (src/fvdb/detail/ops/DownsampleGridMaxPool.cu:19-69,128-230, DownsampleGridAvgPool.cu:19-64,114-201). */
+int fvgb_pool_forward(int32_t mode, int32_t dtype, const FvgbGrid *fine, const FvgbGrid *coarse, const int32_t pool[3],
+                      const int32_t stride[3], const void *x, int64_t ldx, int32_t C, void *y, int64_t ldy,
+                      fvgb_stream_t stream);
+/* Max-pool gradient added into dx_acc [fine n, C] (float for F32/F16/BF16, double for F64;
+ * zero it first): each window's gradient goes to its first strict maximum.  Replaces
+ * DownsampleGridMaxPoolBackward (DownsampleGridMaxPool.cu:71-126,232-326). */
+int fvgb_maxpool_backward(int32_t dtype, const FvgbGrid *fine, const FvgbGrid *coarse, const int32_t pool[3],
+                          const int32_t stride[3], const void *x, int64_t ldx, int32_t C, const void *dy, int64_t lddy,
+                          void *dx_acc, fvgb_stream_t stream);
+/* Average-pool gradient dx [fine n, C] = sum over the windows holding a fine voxel of
+ * dy * 1/(pool volume).  Replaces DownsampleGridAvgPoolBackward (DownsampleGridAvgPool.cu:68-112,203-283). */
+int fvgb_avgpool_backward(int32_t dtype, const FvgbGrid *fine, const FvgbGrid *coarse, const int32_t pool[3],
+                          const int32_t stride[3], int32_t C, const void *dy, int64_t lddy, void *dx, int64_t lddx,
+                          fvgb_stream_t stream);
+/* Nearest upsampling y[f] = x[coarse voxel floor(f / factor)] (zero where there is none), and its
+ * gradient dx[c] = sum of dy over c's children.  Replaces UpsampleGridNearest[Backward]
+ * (src/fvdb/detail/ops/UpsampleGridNearest.cu:19-295). */
+int fvgb_upsample_forward(int32_t dtype, const FvgbGrid *coarse, const FvgbGrid *fine, const int32_t factor[3],
+                          const void *x, int64_t ldx, int32_t C, void *y, int64_t ldy, fvgb_stream_t stream);
+int fvgb_upsample_backward(int32_t dtype, const FvgbGrid *coarse, const FvgbGrid *fine, const int32_t factor[3],
+                           const void *dy, int64_t lddy, int32_t C, void *dx, int64_t lddx, fvgb_stream_t stream);
+/* Candidates of the subdivided grid: voxel c (mask[c] != 0, or all when mask is NULL) gives
+ * c*factor + (i,j,k); out_ijk [n*V, 3], out_valid [n*V] (V = factor volume).  With
+ * fvgb_compact_ijk and a grid build this replaces BuildFineGridFromCoarse
+ * (src/fvdb/detail/ops/BuildFineGridFromCoarse.cu:66-226,343-352). */
+int fvgb_subdivide_candidates(const FvgbGrid *coarse, const int32_t factor[3], const uint8_t *mask, int32_t *out_ijk,
+                              uint8_t *out_valid, fvgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
