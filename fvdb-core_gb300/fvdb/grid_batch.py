@@ -66,6 +66,25 @@ def _per_grid(v, n: int) -> torch.Tensor:
     return t.contiguous()
 
 
+def _as_jagged(data) -> JaggedTensor:
+    if isinstance(data, torch.Tensor):
+        return JaggedTensor(data)
+    if not isinstance(data, JaggedTensor):
+        raise TypeError("data must be a JaggedTensor or a torch.Tensor")
+    return data
+
+
+def _mask_data(mask, grid) -> torch.Tensor | None:
+    if mask is None:
+        return None
+    m = mask.jdata if isinstance(mask, JaggedTensor) else mask
+    if m.dim() != 1 or m.shape[0] != grid.total_voxels:
+        raise ValueError("subdivision mask must be either empty tensor or have one entry per voxel")
+    if m.dtype != torch.bool:
+        raise ValueError("subdivision mask must be a boolean tensor")
+    return m
+
+
 class GridBatch:
     def __init__(self, *, impl):
         self._impl = impl
@@ -178,6 +197,59 @@ class GridBatch:
         if self._halo_pack is None:
             self._halo_pack, _ = self.sparse_conv_kernel_map(3, 1)
         return input.jagged_like(self._halo_pack.sparse_conv_3d(data, weight).jdata)
+
+    # ---------------------------------------------------------------- pooling -----------
+    def coarsened_grid(self, coarsening_factor: Numeric) -> "GridBatch":
+        """Voxels floor(ijk / factor) (fvdb/grid_batch.py:487-501), voxel size factor * w and
+        origin o + (factor - 1) * w / 2."""
+        f = _vec3i(coarsening_factor, "coarsening_factor", positive=True)
+        return GridBatch(impl=self._impl.coarsened_grid(f))
+
+    def subdivided_grid(self, subdiv_factor: Numeric, mask: JaggedTensor | torch.Tensor | None = None) -> "GridBatch":
+        """Every voxel (where `mask` is true) split into factor^3 children (fvdb/grid_batch.py,
+        GridBatch.cpp:645-650), voxel size w / factor and origin o - (factor - 1) * w / (2 factor)."""
+        f = _vec3i(subdiv_factor, "subdiv_factor", positive=True)
+        m = _mask_data(mask, self)
+        return GridBatch(impl=self._impl.subdivided_grid(f, m))
+
+    def max_pool(self, pool_factor: Numeric, data: JaggedTensor, stride: Numeric = 0,
+                 coarse_grid: "GridBatch | None" = None) -> tuple[JaggedTensor, "GridBatch"]:
+        """Max pooling onto `coarse_grid` (default: coarsened_grid(stride)); windows start at
+        coarse ijk * stride and span pool_factor voxels per axis; an empty window is -inf
+        (fvdb/grid_batch.py:1059-1095, GridBatch.cpp:241-274)."""
+        return self._pool(_lib.load().POOL_MAX, pool_factor, data, stride, coarse_grid)
+
+    def avg_pool(self, pool_factor: Numeric, data: JaggedTensor, stride: Numeric = 0,
+                 coarse_grid: "GridBatch | None" = None) -> tuple[JaggedTensor, "GridBatch"]:
+        """Average pooling: the window's sum over its active voxels divided by the window volume
+        (fvdb/grid_batch.py:384-419, GridBatch.cpp:276-310)."""
+        return self._pool(_lib.load().POOL_AVG, pool_factor, data, stride, coarse_grid)
+
+    def _pool(self, mode, pool_factor, data, stride, coarse_grid):
+        from ._pool import PoolFunction
+
+        pf = _vec3i(pool_factor, "pool_factor", positive=True)
+        st = _vec3i(stride, "stride", nonneg=True)
+        st = [s if s > 0 else p for s, p in zip(st, pf)]
+        data = _as_jagged(data)
+        if coarse_grid is None:
+            coarse_grid = self.coarsened_grid(st)
+        out = PoolFunction.apply(mode, self._impl, coarse_grid._impl, pf, st, data.jdata)
+        return coarse_grid.jagged_like(out), coarse_grid
+
+    def subdivide(self, subdiv_factor: Numeric, data: JaggedTensor, mask: JaggedTensor | torch.Tensor | None = None,
+                  fine_grid: "GridBatch | None" = None) -> tuple[JaggedTensor, "GridBatch"]:
+        """Nearest upsampling onto `fine_grid` (default: subdivided_grid(factor, mask)): a fine
+        voxel takes the features of its coarse parent floor(ijk / factor) (fvdb/grid_batch.py:1465-1500,
+        GridBatch.cpp:313-345)."""
+        from ._pool import UpsampleFunction
+
+        f = _vec3i(subdiv_factor, "subdiv_factor", positive=True)
+        data = _as_jagged(data)
+        if fine_grid is None:
+            fine_grid = self.subdivided_grid(f, mask)
+        out = UpsampleFunction.apply(self._impl, fine_grid._impl, f, data.jdata)
+        return fine_grid.jagged_like(out), fine_grid
 
     # ---------------------------------------------------------------- properties --------
     @property

@@ -144,3 +144,67 @@ class RecomputeSequential(nn.Sequential):
         y = checkpoint(run, input.data.jdata, use_reentrant=False)
         out = box["out"]
         return VDBTensor(out.grid, out.grid.jagged_like(y), out.kmap)
+
+
+GridOrVDBTensor = Union[GridBatch, VDBTensor]
+
+
+class MaxPool(nn.Module):
+    """3-D max pooling of a VDBTensor onto a coarser grid (reference: fvdb/nn/modules.py:33-72).
+    Coarse voxels whose window holds no active voxel get 0 (the pooled -inf values are zeroed,
+    as the reference does)."""
+
+    def __init__(self, kernel_size, stride=None):
+        super().__init__()
+        self.kernel_size = kernel_size
+        self.stride = stride or self.kernel_size
+
+    def forward(self, input: VDBTensor, ref_coarse_data: Optional[GridOrVDBTensor] = None) -> VDBTensor:
+        coarse_grid, coarse_kmap = _ref_grid(ref_coarse_data)
+        feat, grid = input.grid.max_pool(self.kernel_size, input.data, stride=self.stride, coarse_grid=coarse_grid)
+        feat.jdata[torch.isinf(feat.jdata)] = 0.0
+        return VDBTensor(grid, feat, kmap=coarse_kmap)
+
+    def extra_repr(self) -> str:
+        return "kernel_size={kernel_size}, stride={stride}".format(kernel_size=self.kernel_size, stride=self.stride)
+
+
+class AvgPool(nn.Module):
+    """3-D average pooling of a VDBTensor onto a coarser grid (reference: fvdb/nn/modules.py:75-106)."""
+
+    def __init__(self, kernel_size, stride=None):
+        super().__init__()
+        self.kernel_size = kernel_size
+        self.stride = stride or self.kernel_size
+
+    def forward(self, input: VDBTensor, ref_coarse_data: Optional[GridOrVDBTensor] = None) -> VDBTensor:
+        coarse_grid, coarse_kmap = _ref_grid(ref_coarse_data)
+        feat, grid = input.grid.avg_pool(self.kernel_size, input.data, stride=self.stride, coarse_grid=coarse_grid)
+        return VDBTensor(grid, feat, kmap=coarse_kmap)
+
+    def extra_repr(self) -> str:
+        return "kernel_size={kernel_size}, stride={stride}".format(kernel_size=self.kernel_size, stride=self.stride)
+
+
+class UpsamplingNearest(nn.Module):
+    """Nearest upsampling of a VDBTensor onto a finer grid (reference: fvdb/nn/modules.py:109-130)."""
+
+    def __init__(self, scale_factor):
+        super().__init__()
+        self.scale_factor = scale_factor
+
+    def forward(self, input: VDBTensor, mask=None, ref_fine_data: Optional[GridOrVDBTensor] = None) -> VDBTensor:
+        fine_grid, fine_kmap = _ref_grid(ref_fine_data)
+        feat, grid = input.grid.subdivide(self.scale_factor, input.data, mask, fine_grid=fine_grid)
+        return VDBTensor(grid, feat, kmap=fine_kmap)
+
+    def extra_repr(self) -> str:
+        return "scale_factor={scale_factor}".format(scale_factor=self.scale_factor)
+
+
+def _ref_grid(ref):
+    if isinstance(ref, VDBTensor):
+        return ref.grid, ref.kmap
+    if isinstance(ref, GridBatch):
+        return ref, None
+    return None, None

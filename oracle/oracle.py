@@ -225,3 +225,137 @@ def gs_forward(x, weight, nbmap: np.ndarray, nbsizes: np.ndarray, n_out: int, tr
         scatter(n, cout, ctypes.c_void_p(o.data_ptr()), ctypes.c_void_p(out.data_ptr()), _p(seg), scol)
         cur += n
     return out
+
+
+# ----------------------------------------------------------------------- pooling ---------
+# Restatement of the reference's pooling / nearest-upsampling loops (src/fvdb/detail/ops/
+# DownsampleGridMaxPool.cu:19-126, DownsampleGridAvgPool.cu:19-112,144,
+# UpsampleGridNearest.cu:19-110, BuildFineGridFromCoarse.cu:66-226,
+# CoarseIjkForFineGrid.cu:19-41) on numpy arrays.  Coordinates must lie in [-2048, 2048).
+def _coord_keys(ijk: np.ndarray, joff) -> np.ndarray:
+    ijk = np.asarray(ijk, dtype=np.int64).reshape(-1, 3)
+    assert ijk.size == 0 or (ijk.min() >= -2048 and ijk.max() < 2048)
+    b = np.repeat(np.arange(len(joff) - 1), np.diff(np.asarray(joff)))
+    return (b << 36) | ((ijk[:, 0] + 2048) << 24) | ((ijk[:, 1] + 2048) << 12) | (ijk[:, 2] + 2048)
+
+
+def _lookup(ijk: np.ndarray, joff, q_ijk: np.ndarray, q_batch: np.ndarray) -> np.ndarray:
+    """Row of each query coordinate in the grid (ijk, joff), or -1."""
+    keys = _coord_keys(ijk, joff)
+    order = np.argsort(keys)
+    sk = keys[order]
+    q = np.asarray(q_ijk, dtype=np.int64)
+    ok = np.all((q >= -2048) & (q < 2048), axis=1)
+    qk = (q_batch.astype(np.int64) << 36) | ((q[:, 0] + 2048) << 24) | ((q[:, 1] + 2048) << 12) | (q[:, 2] + 2048)
+    pos = np.searchsorted(sk, qk)
+    pos = np.minimum(pos, max(sk.size - 1, 0))
+    hit = ok & (sk.size > 0) & (sk[pos] == qk) if sk.size else np.zeros(qk.shape, bool)
+    return np.where(hit, order[pos] if sk.size else 0, -1)
+
+
+def _batch_of(joff) -> np.ndarray:
+    return np.repeat(np.arange(len(joff) - 1), np.diff(np.asarray(joff)))
+
+
+def coarsened_grid(ijk, joff, factor):
+    """floor(ijk / factor) per grid, in index order (CoarseIjkForFineGrid.cu:19-41)."""
+    f = np.asarray(_vec3(factor), dtype=np.int64)
+    c = np.floor_divide(np.asarray(ijk, dtype=np.int64), f).astype(np.int32)
+    return grid_from_ijk(c, np.asarray(joff))
+
+
+def subdivided_grid(ijk, joff, factor, mask=None):
+    """Every (masked) voxel c split into c*factor + (i,j,k) (BuildFineGridFromCoarse.cu:66-226)."""
+    f = _vec3(factor).astype(np.int64)
+    ijk = np.asarray(ijk, dtype=np.int64)
+    keep = np.ones(ijk.shape[0], bool) if mask is None else np.asarray(mask, bool)
+    off = np.stack(np.meshgrid(np.arange(f[0]), np.arange(f[1]), np.arange(f[2]), indexing="ij"), -1).reshape(-1, 3)
+    parts, counts = [], []
+    for b in range(len(joff) - 1):
+        sel = ijk[joff[b]:joff[b + 1]][keep[joff[b]:joff[b + 1]]]
+        ch = (sel[:, None, :] * f + off[None]).reshape(-1, 3)
+        parts.append(ch)
+        counts.append(ch.shape[0])
+    cand = np.concatenate(parts).astype(np.int32) if parts else np.zeros((0, 3), np.int32)
+    return grid_from_ijk(cand, np.concatenate([[0], np.cumsum(counts)]).astype(np.int64))
+
+
+def _windows(base: np.ndarray, ext):
+    for i in range(ext[0]):
+        for j in range(ext[1]):
+            for k in range(ext[2]):
+                yield base + np.array([i, j, k], dtype=np.int64)
+
+
+def pool_forward(fine_ijk, fine_off, coarse_ijk, coarse_off, x: np.ndarray, pool, stride, mode: str) -> np.ndarray:
+    """mode "max": max over the window's active fine voxels (-inf when none); "avg": window sum
+    in x's precision (window order i-outer, k-inner) times (1 / pool volume) in that precision."""
+    p, s = _vec3(pool).astype(np.int64), _vec3(stride).astype(np.int64)
+    s = np.where(s == 0, p, s)
+    base = np.asarray(coarse_ijk, dtype=np.int64) * s
+    cb = _batch_of(coarse_off)
+    dt = x.dtype
+    acc = np.full((base.shape[0], x.shape[1]), -np.inf if mode == "max" else 0.0, dtype=dt)
+    for q in _windows(base, p):
+        r = _lookup(fine_ijk, fine_off, q, cb)
+        v = r >= 0
+        if mode == "max":
+            acc[v] = np.fmax(x[r[v]], acc[v])
+        else:
+            acc[v] = acc[v] + x[r[v]]
+    if mode == "avg":
+        acc = acc * dt.type(1.0 / float(np.prod(p)))
+    return acc
+
+
+def pool_backward(fine_ijk, fine_off, coarse_ijk, coarse_off, x: np.ndarray, dy: np.ndarray, pool, stride,
+                  mode: str) -> np.ndarray:
+    """Max: each window's gradient goes to its first strict maximum; average: dy * (1 / volume)
+    to every active voxel of the window (DownsampleGridMaxPool.cu:71-126, DownsampleGridAvgPool.cu:68-112)."""
+    p, s = _vec3(pool).astype(np.int64), _vec3(stride).astype(np.int64)
+    s = np.where(s == 0, p, s)
+    base = np.asarray(coarse_ijk, dtype=np.int64) * s
+    cb = _batch_of(coarse_off)
+    dx = np.zeros_like(x)
+    if mode == "max":
+        best = np.full(dy.shape, -np.inf, dtype=x.dtype)
+        arg = np.full(dy.shape, -1, dtype=np.int64)
+        for q in _windows(base, p):
+            r = _lookup(fine_ijk, fine_off, q, cb)
+            v = r >= 0
+            vals = np.where(v[:, None], x[np.maximum(r, 0)], -np.inf)
+            upd = vals > best
+            best = np.where(upd, vals, best)
+            arg = np.where(upd, r[:, None], arg)
+        rows, cols = np.nonzero(arg >= 0)
+        np.add.at(dx, (arg[rows, cols], cols), dy[rows, cols])
+        return dx
+    g = dy * dy.dtype.type(1.0 / float(np.prod(p)))
+    for q in _windows(base, p):
+        r = _lookup(fine_ijk, fine_off, q, cb)
+        v = r >= 0
+        np.add.at(dx, r[v], g[v])
+    return dx
+
+
+def upsample_forward(coarse_ijk, coarse_off, fine_ijk, fine_off, x: np.ndarray, factor) -> np.ndarray:
+    """Fine voxel f takes coarse voxel floor(f / factor) (zero without one)."""
+    f = _vec3(factor).astype(np.int64)
+    par = np.floor_divide(np.asarray(fine_ijk, dtype=np.int64), f)
+    r = _lookup(coarse_ijk, coarse_off, par, _batch_of(fine_off))
+    out = np.zeros((par.shape[0], x.shape[1]), dtype=x.dtype)
+    out[r >= 0] = x[r[r >= 0]]
+    return out
+
+
+def upsample_backward(coarse_ijk, coarse_off, fine_ijk, fine_off, dy: np.ndarray, factor) -> np.ndarray:
+    """Coarse voxel c sums the gradients of its children c*factor + (i,j,k) in window order."""
+    f = _vec3(factor).astype(np.int64)
+    base = np.asarray(coarse_ijk, dtype=np.int64) * f
+    cb = _batch_of(coarse_off)
+    dx = np.zeros((base.shape[0], dy.shape[1]), dtype=dy.dtype)
+    for q in _windows(base, f):
+        r = _lookup(fine_ijk, fine_off, q, cb)
+        v = r >= 0
+        dx[v] = dx[v] + dy[r[v]]
+    return dx
