@@ -185,7 +185,7 @@ def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) ->
     def planned(y):
         rc = lib.fvgb_conv_fwd_tc_planned(2, P(x), ctypes.c_int64(n), cin, ctypes.c_int64(x.stride(0)), P(plan),
                                           ctypes.c_int64(n), K, P(packed), cout, P(y), ctypes.c_int64(cout), None,
-                                          None, P(err), stream)
+                                          None, 0, P(err), stream)
         assert rc == 0, rc
 
     def unplanned(y):
@@ -571,7 +571,8 @@ def leg_train(fvdb, dev, args) -> dict:
         d = dy.to(dev, dtype)
 
         def step():
-            h = torch.relu(pack.sparse_conv_3d(x, a).jdata)
+            # conv -> ReLU (fused into the first convolution's epilogue) -> conv
+            h = pack._conv_with_bias(x, a, None, False, None, relu=True).jdata
             y = pack.sparse_conv_3d(h, b).jdata
             x.grad = a.grad = b.grad = None
             y.backward(d)

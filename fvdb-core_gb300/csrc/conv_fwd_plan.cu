@@ -262,6 +262,7 @@ struct PlanArgs {
     int64_t ldy;
     const float *scale;
     const float *bias;
+    int32_t relu;  // 1: max(., 0) after the bias (fused activation)
     int32_t *err;
     int64_t n_tiles;
     int32_t direct_store;
@@ -572,6 +573,10 @@ __global__ void __launch_bounds__(kThreadsP, 1) conv_plan_fwd_kernel(PlanArgs a)
                         lo += cc < a.cout ? a.bias[cc] : 0.f;
                         hi += cc + 1 < a.cout ? a.bias[cc + 1] : 0.f;
                     }
+                    if (a.relu) {  // NaN passes through, as torch.relu
+                        lo = lo < 0.f ? 0.f : lo;
+                        hi = hi < 0.f ? 0.f : hi;
+                    }
                     __nv_bfloat162 h2 = __floats2bfloat162_rn(lo, hi);
                     packed[t] = *reinterpret_cast<uint32_t *>(&h2);
                 }
@@ -817,7 +822,7 @@ extern "C" int fvgb_tc_plan_build(const int32_t *map, int64_t n_rows, int32_t K,
 extern "C" int fvgb_conv_fwd_tc_planned(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
                                         const void *plan, int64_t n_out, int32_t K, const void *packed_w,
                                         int32_t c_out, void *y, int64_t ldy, const float *out_scale,
-                                        const float *bias, int32_t *err_dev, fvgb_stream_t stream) {
+                                        const float *bias, int32_t relu, int32_t *err_dev, fvgb_stream_t stream) {
     int st = fvgb_tc_plan_supported(dtype, K, c_in, c_out);
     if (st) return st;
     const int eb = dtype == FVGB_E4M3 ? 1 : 2;
@@ -848,6 +853,7 @@ extern "C" int fvgb_conv_fwd_tc_planned(int32_t dtype, const void *x, int64_t n_
     a.ldy = ldy;
     a.scale = out_scale;
     a.bias = bias;
+    a.relu = relu ? 1 : 0;
     a.err = err_dev;
     a.n_tiles = L.n_tiles;
     a.direct_store = (ldy == c_out && c_out % 8 == 0) ? 1 : 0;

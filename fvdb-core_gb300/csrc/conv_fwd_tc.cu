@@ -84,6 +84,7 @@ struct FwdArgs {
     int64_t ldy;
     const float *scale;         // per output channel, may be null
     const float *bias;          // per output channel, added after the scale, may be null
+    int32_t relu;               // 1: max(., 0) after the bias (fused activation)
     int32_t *err;
     int32_t stages;
     int64_t n_tiles;
@@ -412,6 +413,10 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                         lo += cc < a.cout ? a.bias[cc] : 0.f;
                         hi += cc + 1 < a.cout ? a.bias[cc + 1] : 0.f;
                     }
+                    if (a.relu) {  // NaN passes through, as torch.relu
+                        lo = lo < 0.f ? 0.f : lo;
+                        hi = hi < 0.f ? 0.f : hi;
+                    }
                     __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
                     packed[t] = *reinterpret_cast<uint32_t *>(&h);
                 }
@@ -658,6 +663,15 @@ extern "C" int fvgb_conv_fwd_tc_bias(int32_t dtype, const void *x, int64_t n_x, 
                                      const void *packed_w, int32_t c_out, void *y, int64_t ldy,
                                      const float *out_scale, const float *bias, int32_t *err_dev,
                                      fvgb_stream_t stream) {
+    return fvgb_conv_fwd_tc_epilogue(dtype, x, n_x, c_in, ldx, map, n_out, K, tile_mask, packed_w, c_out, y, ldy,
+                                     out_scale, bias, 0, err_dev, stream);
+}
+
+extern "C" int fvgb_conv_fwd_tc_epilogue(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                         const int32_t *map, int64_t n_out, int32_t K, const uint32_t *tile_mask,
+                                         const void *packed_w, int32_t c_out, void *y, int64_t ldy,
+                                         const float *out_scale, const float *bias, int32_t relu, int32_t *err_dev,
+                                         fvgb_stream_t stream) {
     const int eb = dtype == FVGB_E4M3 ? 1 : (dtype == FVGB_BF16 ? 2 : 0);
     if (!eb) return FVGB_ETYPE;
     if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldx < c_in || ldy < c_out || !err_dev)
@@ -695,6 +709,7 @@ extern "C" int fvgb_conv_fwd_tc_bias(int32_t dtype, const void *x, int64_t n_x, 
     a.ldy = ldy;
     a.scale = out_scale;
     a.bias = bias;
+    a.relu = relu ? 1 : 0;
     a.err = err_dev;
     a.stages = 0;
     a.n_tiles = ceil_div(n_out, kTileM);

@@ -620,7 +620,8 @@ bool use_tensor_cores(const Tensor &x, int64_t cin, int64_t cout) {
 // with them, shapes the planned kernel takes run over the pack's cached tile plan.
 Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &Wkio, bool transpose_w,
                    const std::optional<Tensor> &tile_mask = std::nullopt,
-                   const std::optional<Tensor> &bias = std::nullopt, PackPtr pack = nullptr, bool map_t = false) {
+                   const std::optional<Tensor> &bias = std::nullopt, PackPtr pack = nullptr, bool map_t = false,
+                   bool relu = false) {
     c10::cuda::CUDAGuard guard(x.device());
     const int64_t K = map.size(1);
     const int64_t cin = transpose_w ? Wkio.size(2) : Wkio.size(1);
@@ -648,16 +649,16 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
             check_status(fvgb_conv_fwd_tc_planned(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
                                                   plan->data_ptr(), n_out, (int32_t)K, packed.data_ptr(),
                                                   (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
-                                                  bias ? b32.data_ptr<float>() : nullptr,
+                                                  bias ? b32.data_ptr<float>() : nullptr, relu ? 1 : 0,
                                                   device_error_flag(x.device()).data_ptr<int32_t>(), s),
                          "sparse conv forward (tensor cores)");
             return y;
         }
-        check_status(fvgb_conv_fwd_tc_bias(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
-                                           map.data_ptr<int32_t>(), n_out, (int32_t)K, tm, packed.data_ptr(),
-                                           (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
-                                           bias ? b32.data_ptr<float>() : nullptr,
-                                           device_error_flag(x.device()).data_ptr<int32_t>(), s),
+        check_status(fvgb_conv_fwd_tc_epilogue(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
+                                               map.data_ptr<int32_t>(), n_out, (int32_t)K, tm, packed.data_ptr(),
+                                               (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
+                                               bias ? b32.data_ptr<float>() : nullptr, relu ? 1 : 0,
+                                               device_error_flag(x.device()).data_ptr<int32_t>(), s),
                      "sparse conv forward (tensor cores)");
         return y;
     } else if (dt == FVGB_F32 || dt == FVGB_F64) {
@@ -679,6 +680,7 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
         y.copy_(yf);
     }
     if (bias) y.add_(bias->to(y.scalar_type()));
+    if (relu) y.relu_();
     return y;
 }
 
@@ -721,8 +723,9 @@ Tensor gather_wgrad(const Tensor &x, const Tensor &map, int64_t n_out, const Ten
 // ------------------------------------------------------------------------------------------
 // Forward / backward of one sparse convolution, called by the Python autograd Function.
 // Checks and permutes follow SparseConvolutionKernelMap.cpp:18-191.
+// relu: the output is max(conv + bias, 0), fused into the tensor-core epilogue.
 std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed,
-                                 const std::optional<Tensor> &bias = std::nullopt) {
+                                 const std::optional<Tensor> &bias = std::nullopt, bool relu = false) {
     TORCH_CHECK_VALUE(x.is_contiguous(), "features must be contiguous");
     TORCH_CHECK_TYPE(x.is_floating_point(), "features must have a floating point type");
     TORCH_CHECK_VALUE(x.dim() == 2, "Expected features to have 2 dimensions (shape (n, nF)) but got ", x.dim(),
@@ -760,10 +763,10 @@ std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr
     }
     Tensor y;
     if (!transposed)
-        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false), bias, p, false)
+        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false), bias, p, false, relu)
                       : torch::empty({0, cout}, x.options());
     else
-        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true), bias, p, true)
+        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true), bias, p, true, relu)
                       : torch::empty({0, cout}, x.options());
     return {y, Wkio};
 }
@@ -795,7 +798,8 @@ std::vector<Tensor> conv_backward(const Tensor &dy_in, const Tensor &x, const Te
 // and per-output-channel weight scales s_w (applied in the epilogue), FP32 accumulation:
 //   y[m, co] = s_w[co] * sum_k sum_ci e4m3(x[., ci] / s_x[ci]) * e4m3(s_x[ci] W[k, ci, co] / s_w[co])
 // Returns (y bf16, s_x, s_w).
-std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed) {
+std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed,
+                                     bool relu = false) {
     TORCH_CHECK_VALUE(x.dim() == 2 && x.is_cuda() && x.is_floating_point(), "features must be a 2-D CUDA float tensor");
     TORCH_CHECK_VALUE(weights.dim() == 5, "Expected kernels to have 5 dimensions");
     c10::cuda::CUDAGuard guard(x.device());
@@ -839,15 +843,17 @@ std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, Pac
     if (plan) {
         check_status(fvgb_conv_fwd_tc_planned(FVGB_E4M3, x8.data_ptr(), x8.size(0), (int32_t)cin, cin, plan->data_ptr(),
                                               n_rows, (int32_t)K, packed.data_ptr(), (int32_t)cout, y.data_ptr(),
-                                              y.stride(0), sw.data_ptr<float>(), nullptr,
+                                              y.stride(0), sw.data_ptr<float>(), nullptr, relu ? 1 : 0,
                                               device_error_flag(x.device()).data_ptr<int32_t>(), s),
                      "sparse conv forward (fp8 tensor cores)");
         return {y, s_x, s_w};
     }
-    check_status(fvgb_conv_fwd_tc(FVGB_E4M3, x8.data_ptr(), x8.size(0), (int32_t)cin, cin, map.data_ptr<int32_t>(), n_rows,
-                                  (int32_t)K, tm ? reinterpret_cast<const uint32_t *>(tm->data_ptr<int32_t>()) : nullptr,
-                                  packed.data_ptr(), (int32_t)cout, y.data_ptr(), y.stride(0), sw.data_ptr<float>(),
-                                  device_error_flag(x.device()).data_ptr<int32_t>(), s),
+    check_status(fvgb_conv_fwd_tc_epilogue(FVGB_E4M3, x8.data_ptr(), x8.size(0), (int32_t)cin, cin,
+                                           map.data_ptr<int32_t>(), n_rows, (int32_t)K,
+                                           tm ? reinterpret_cast<const uint32_t *>(tm->data_ptr<int32_t>()) : nullptr,
+                                           packed.data_ptr(), (int32_t)cout, y.data_ptr(), y.stride(0),
+                                           sw.data_ptr<float>(), nullptr, relu ? 1 : 0,
+                                           device_error_flag(x.device()).data_ptr<int32_t>(), s),
                  "sparse conv forward (fp8 tensor cores)");
     return {y, s_x, s_w};
 }
@@ -1073,8 +1079,10 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     // the GIL is released while the native calls run (their grid builds wait for a count read),
     // so host threads of concurrent serving slots do not serialise on it
     m.def("conv_forward", &conv_forward, py::arg("features"), py::arg("weights"), py::arg("pack"),
-          py::arg("transposed"), py::arg("bias") = py::none(), py::call_guard<py::gil_scoped_release>());
-    m.def("conv_forward_fp8", &conv_forward_fp8, py::call_guard<py::gil_scoped_release>());
+          py::arg("transposed"), py::arg("bias") = py::none(), py::arg("relu") = false,
+          py::call_guard<py::gil_scoped_release>());
+    m.def("conv_forward_fp8", &conv_forward_fp8, py::arg("features"), py::arg("weights"), py::arg("pack"),
+          py::arg("transposed"), py::arg("relu") = false, py::call_guard<py::gil_scoped_release>());
     m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); },
           py::call_guard<py::gil_scoped_release>());
     m.def("conv_backward", &conv_backward, py::call_guard<py::gil_scoped_release>());

@@ -79,7 +79,7 @@ class SparseConv3d(nn.Module):
         if self.bias is not None:
             self.bias.data.uniform_(-std, std)
 
-    def _dispatch_conv(self, in_feature, in_grid: GridBatch, in_kmap, out_grid):
+    def _dispatch_conv(self, in_feature, in_grid: GridBatch, in_kmap, out_grid, relu: bool = False):
         can_cache = self.stride == (1, 1, 1) and (out_grid is None or out_grid.is_same(in_grid))
         if in_kmap is not None and in_kmap.kernel_size == self.kernel_size and can_cache:
             kmap, out_grid = in_kmap, in_grid
@@ -94,18 +94,22 @@ class SparseConv3d(nn.Module):
             kmap.build_implicit_gemm(sorted=False, training=False)
         prec = None if self.precision == "native" else self.precision
         # the bias is added in the contraction's epilogue (the reference adds it in a second pass)
-        out_feature = kmap._conv_with_bias(in_feature, self.weight, self.bias, self.transposed, prec)
+        out_feature = kmap._conv_with_bias(in_feature, self.weight, self.bias, self.transposed, prec, relu)
         return out_grid, out_feature, out_kmap
 
-    def forward(self, input: VDBTensor, out_grid: Optional[GridBatch] = None) -> VDBTensor:
+    def forward(self, input: VDBTensor, out_grid: Optional[GridBatch] = None, *, relu: bool = False) -> VDBTensor:
+        """`relu` (extension): return max(conv(input) + bias, 0), the clamp fused into the
+        contraction's epilogue (nn.Sequential passes it for a SparseConv3d followed by a ReLU)."""
         in_feature, in_grid, in_kmap = input.data, input.grid, input.kmap
         if self.kernel_size == (1, 1, 1) and self.stride == (1, 1, 1):
             out_feature = in_feature.jagged_like(in_feature.jdata.matmul(self.weight.transpose(0, 1)))
             out_grid, out_kmap = in_grid, in_kmap
             if self.bias is not None:
                 out_feature.jdata = out_feature.jdata + self.bias
+            if relu:
+                out_feature.jdata = torch.relu(out_feature.jdata)
         else:
-            out_grid, out_feature, out_kmap = self._dispatch_conv(in_feature, in_grid, in_kmap, out_grid)
+            out_grid, out_feature, out_kmap = self._dispatch_conv(in_feature, in_grid, in_kmap, out_grid, relu)
         if out_grid is None:
             raise ValueError("Failed to compute output grid. This is a bug in the implementation.")
         return VDBTensor(out_grid, out_feature, out_kmap)
@@ -119,7 +123,23 @@ class ReLU(nn.ReLU):
 
 
 class Sequential(nn.Sequential):
-    """nn.Sequential over VDBTensor-to-VDBTensor layers."""
+    """nn.Sequential over VDBTensor-to-VDBTensor layers.  A SparseConv3d directly followed by a
+    ReLU runs as one convolution with the ReLU fused into its epilogue: the same values (rounding
+    to the output type keeps signs) and gradients, one pass over the output instead of two."""
+
+    def forward(self, input):
+        mods = list(self)
+        i = 0
+        while i < len(mods):
+            m = mods[i]
+            nxt = mods[i + 1] if i + 1 < len(mods) else None
+            if isinstance(m, SparseConv3d) and type(nxt) is ReLU and not nxt.inplace:
+                input = m(input, relu=True)
+                i += 2
+                continue
+            input = m(input)
+            i += 1
+        return input
 
 
 class RecomputeSequential(nn.Sequential):

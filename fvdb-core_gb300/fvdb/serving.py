@@ -248,9 +248,8 @@ class ConvStack:
         pack, _ = grid.sparse_conv_kernel_map(self.kernel_size, 1)
         h = x.to(self.dtype)
         for i, w in enumerate(self.weights):
-            h = pack.sparse_conv_3d(h, w).jdata
-            if i + 1 < len(self.weights):
-                h = torch.relu(h)
+            # ReLU between layers, fused into the convolution's epilogue
+            h = pack._conv_with_bias(h, w, None, False, None, relu=i + 1 < len(self.weights)).jdata
         return h
 
 

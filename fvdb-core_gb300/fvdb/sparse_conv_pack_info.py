@@ -51,11 +51,12 @@ def _vec(v) -> list[int]:
 
 
 def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, precision: str | None,
-           bias: torch.Tensor | None = None) -> torch.Tensor:
+           bias: torch.Tensor | None = None, relu: bool = False) -> torch.Tensor:
     """One convolution in the requested arithmetic.  The result has the dtype that the
     reference's `conv(x) + bias` has (torch type promotion of the contraction's output and the
     bias): the bias is fused into the contraction's epilogue when that dtype is the output's
-    own, and added afterwards (promoting) otherwise."""
+    own, and added afterwards (promoting) otherwise.  `relu` applies max(., 0) last, fused into
+    the epilogue with the bias."""
     if precision in (None, "native"):
         x, w = data, weights
     elif precision == "bf16":
@@ -64,13 +65,19 @@ def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, pr
         if torch.is_grad_enabled() and (data.requires_grad or weights.requires_grad or
                                         (bias is not None and bias.requires_grad)):
             raise RuntimeError("the FP8 convolution is forward-only; use precision='bf16' for training")
-        y, _, _ = _lib.load().conv_forward_fp8(data, weights, impl, transposed)
-        return y if bias is None else y + bias
+        fuse = bias is None
+        y, _, _ = _lib.load().conv_forward_fp8(data, weights, impl, transposed, relu and fuse)
+        if bias is not None:
+            y = y + bias
+            if relu:
+                y = torch.relu(y)
+        return y
     else:
         raise ValueError(f"precision must be one of None, 'native', 'bf16', 'fp8' (got {precision!r})")
     if bias is not None and torch.result_type(x, bias) != x.dtype:
-        return sparse_conv(x, w, impl, transposed, None) + bias
-    return sparse_conv(x, w, impl, transposed, bias)
+        y = sparse_conv(x, w, impl, transposed, None) + bias
+        return torch.relu(y) if relu else y
+    return sparse_conv(x, w, impl, transposed, bias, relu)
 
 
 class SparseConvPackInfo:
@@ -167,13 +174,14 @@ class SparseConvPackInfo:
         return JaggedTensor.from_data_and_offsets(out, self._impl.source_grid.joffsets)
 
     def _conv_with_bias(self, input, weights: torch.Tensor, bias: torch.Tensor | None, transposed: bool,
-                        precision: str | None = None) -> JaggedTensor:
-        """sparse_conv_3d / sparse_transpose_conv_3d plus a per-output-channel bias added in the
-        contraction's epilogue (used by nn.SparseConv3d)."""
+                        precision: str | None = None, relu: bool = False) -> JaggedTensor:
+        """sparse_conv_3d / sparse_transpose_conv_3d plus a per-output-channel bias (and, with
+        `relu`, max(., 0)) applied in the contraction's epilogue (used by nn.SparseConv3d and
+        nn.Sequential's conv -> ReLU fusion)."""
         src, tgt = self._impl.source_grid, self._impl.target_grid
         inp, out = (tgt, src) if transposed else (src, tgt)
         data = self._features(input, inp.grid_count, inp.total_voxels)
-        y = _apply(data, weights, self._impl, transposed, precision, bias)
+        y = _apply(data, weights, self._impl, transposed, precision, bias, relu)
         return JaggedTensor.from_data_and_offsets(y, out.joffsets)
 
     # ---------------------------------------------------------------- devices -----------

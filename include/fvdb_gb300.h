@@ -326,6 +326,17 @@ int fvgb_conv_fwd_tc_bias(int32_t dtype, const void *x, int64_t n_x, int32_t c_i
                           fvgb_stream_t stream);
 
 /*
+ * fvgb_conv_fwd_tc_bias with a fused activation: relu != 0 clamps every output at zero after the
+ * scale and the bias (NaN passes through), so conv -> ReLU writes its output once.  Rounding to
+ * BF16 keeps signs, so the result equals ReLU applied to fvgb_conv_fwd_tc_bias's output.  The
+ * reference applies fvdb.nn.ReLU as a separate pass (fvdb/nn/modules.py, torch.nn.ReLU on jdata).
+ */
+int fvgb_conv_fwd_tc_epilogue(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                              const int32_t *map, int64_t n_out, int32_t K, const uint32_t *tile_mask,
+                              const void *packed_w, int32_t c_out, void *y, int64_t ldy, const float *out_scale,
+                              const float *bias, int32_t relu, int32_t *err_dev, fvgb_stream_t stream);
+
+/*
  * Tile plan of a kernel map for the planned tensor-core convolution: for every 128-row tile of
  * `map` ([ceil(n_rows/128)*128, K] int32, -1 = absent, K <= 32) the distinct source rows it
  * reads (split into phases that fit the kernel's staging buffer, which depends on row_bytes =
@@ -347,15 +358,15 @@ int fvgb_tc_plan_supported(int32_t dtype, int32_t K, int32_t c_in, int32_t c_out
  * row_bytes = c_in * element size): each tile's distinct input rows are staged in shared memory
  * once and the gathered A operand is assembled in tensor memory, so no map entry is gathered
  * from L2 on its own.  Same arguments, weight image, result and error flag as
- * fvgb_conv_fwd_tc_bias (the map and tile masks are read from the plan).  Replaces
+ * fvgb_conv_fwd_tc_epilogue (the map and tile masks are read from the plan).  Replaces
  * dispatchSparseConvolutionImplicitGEMM[Sorted]<kCUDA>
  * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionImplicitGEMM.cu:2754-3826,
  * SparseConvolutionImplicitGEMMSorted.cu:3101-4641).
  */
 int fvgb_conv_fwd_tc_planned(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
                              const void *plan, int64_t n_out, int32_t K, const void *packed_w, int32_t c_out,
-                             void *y, int64_t ldy, const float *out_scale, const float *bias, int32_t *err_dev,
-                             fvgb_stream_t stream);
+                             void *y, int64_t ldy, const float *out_scale, const float *bias, int32_t relu,
+                             int32_t *err_dev, fvgb_stream_t stream);
 
 /*
  * Tensor-core weight gradient, BF16 operands:  dw[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co]

@@ -214,7 +214,7 @@ def test_planned_through_c_abi_equals_unplanned(cuda_device, case, cin, cout):
     y2 = torch.empty_like(y1)
     assert lib.fvgb_conv_fwd_tc_planned(2, P(x), ctypes.c_int64(n_in), cin, ctypes.c_int64(cin), P(plan),
                                         ctypes.c_int64(n_out), K, P(packed), cout, P(y1), ctypes.c_int64(cout),
-                                        None, P(bias), P(err), stream) == 0
+                                        None, P(bias), 0, P(err), stream) == 0
     assert lib.fvgb_conv_fwd_tc_bias(2, P(x), ctypes.c_int64(n_in), cin, ctypes.c_int64(cin), P(kmap),
                                      ctypes.c_int64(n_out), K, None, P(packed), cout, P(y2), ctypes.c_int64(cout),
                                      None, P(bias), P(err), stream) == 0
