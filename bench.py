@@ -451,6 +451,8 @@ def run_gpu(args) -> None:
         line["bf16_vs_fp32"] = tf / line["fp32_plain"]["value"] if line["fp32_plain"]["value"] else None
     if "c1" in legs:
         line["c1_fp32"] = leg_c1(fvdb, dev, args)
+    if "halo" in legs:
+        line["halo_l1"] = leg_halo(fvdb, grid, x, model, args)
     if "train" in legs:
         line["train_c3"] = leg_train(fvdb, dev, args)
     if "fp8" in legs:
@@ -501,8 +503,40 @@ def leg_fp32(fvdb, grid, x, model, flops, args) -> dict:
     p2, _ = grid.sparse_conv_kernel_map(2, 2)
     y64 = p2.sparse_conv_3d(p1.sparse_conv_3d(x.double(), model.w1.double()).jdata, model.w2.double()).jdata
     y32 = p2.sparse_conv_3d(p1.sparse_conv_3d(xf, w1).jdata, w2).jdata
+    # the layer-1 FP32 contraction alone (map prebuilt) against the measured FFMA rate
+    P1 = int((p1.out_in_map >= 0).sum())
+    l1_ms = time_ms(lambda: p1.sparse_conv_3d(xf, w1), max(3, args.steps // 2), 2)
+    l1_tflops = 2.0 * P1 * 32 * 64 / (l1_ms * 1e-3) / 1e12
+    peak = ffma_peak_tflops()
     return {"value": flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms, "dtype": "f32",
+            "layer1_contraction_ms": l1_ms, "layer1_contraction_tflops": l1_tflops,
+            "ffma_peak_tflops": peak, "layer1_frac_of_ffma_peak": l1_tflops / peak if peak else None,
             "errors_vs_fp64": {"bf16_step": rel_errors(y16, y64), "fp32_step": rel_errors(y32, y64)}}
+
+
+def ffma_peak_tflops() -> float:
+    """FP32 FMA rate of this GPU: the library's probe kernel (8 independent fma chains per
+    thread, 8 CTAs of 256 threads per SM) timed with CUDA events, best of 3."""
+    import ctypes
+
+    from fvdb import _lib
+
+    lib = _lib.cdll()
+    out = torch.zeros(2, device="cuda")
+    flops = ctypes.c_double(0.0)
+    stream = torch.cuda.current_stream().cuda_stream
+    best = 0.0
+    for _ in range(4):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        rc = lib.fvgb_ffma_probe(ctypes.c_void_p(out.data_ptr()), ctypes.c_int64(1 << 16), 8, ctypes.byref(flops),
+                                 ctypes.c_void_p(stream))
+        b.record()
+        torch.cuda.synchronize()
+        if rc != 0:
+            return 0.0
+        best = max(best, flops.value / (a.elapsed_time(b) * 1e-3) / 1e12)
+    return best
 
 
 def leg_c1(fvdb, dev, args) -> dict:
@@ -528,6 +562,53 @@ def leg_c1(fvdb, dev, args) -> dict:
     return {"voxels": grid.total_voxels, "pairs": P, "ms_per_step": ms, "us_per_step": ms * 1e3,
             "voxels_per_s": grid.total_voxels / (ms * 1e-3), "useful_tflops": 2.0 * P * 16 * 16 / (ms * 1e-3) / 1e12,
             "dtype": "f32", "errors_vs_fp64": rel_errors(y32, y64)}
+
+
+def leg_halo(fvdb, grid, x, model, args) -> dict:
+    """Layer 1 of the headline step (3^3, stride 1, 32 -> 64) through GridBatch.sparse_conv_halo
+    (leaf-halo kernels, no kernel map) beside the kernel-map path (map build included), BF16 and
+    FP32, forward and forward + backward; errors of each against FP64.  On the headline's
+    sphere-shell grids and on a dense 96^3 block (every leaf full)."""
+    dev = x.device
+    r = torch.arange(96, dtype=torch.int32, device=dev)
+    dense = fvdb.GridBatch.from_ijk(torch.stack(torch.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3))
+    xd_dense = torch.randn(dense.total_voxels, 32, generator=torch.Generator().manual_seed(3)).to(dev, torch.bfloat16)
+    out = {}
+    for gname, gg, xx in (("shells", grid, x), ("dense96", dense, xd_dense)):
+        w64 = model.w1.double()
+        p1, _ = gg.sparse_conv_kernel_map(3, 1)
+        y64 = p1.sparse_conv_3d(xx.double(), w64).jdata
+        res = {"voxels": gg.total_voxels}
+        for name, dt in (("bf16", torch.bfloat16), ("fp32", torch.float32)):
+            xd, wd = xx.to(dt), model.w1.to(dt)
+            jx = gg.jagged_like(xd)
+
+            def halo_fwd():
+                return gg.sparse_conv_halo(jx, wd).jdata
+
+            def map_fwd():
+                p, _ = gg.sparse_conv_kernel_map(3, 1)
+                return p.sparse_conv_3d(xd, wd).jdata
+
+            xg, wg = xd.clone().requires_grad_(True), wd.clone().requires_grad_(True)
+            jg = gg.jagged_like(xg)
+            dy = torch.ones(gg.total_voxels, wd.shape[0], device=dev, dtype=dt)
+
+            def halo_train():
+                gg.sparse_conv_halo(jg, wg).jdata.backward(dy)
+
+            def map_train():
+                p, _ = gg.sparse_conv_kernel_map(3, 1)
+                p.sparse_conv_3d(xg, wg).jdata.backward(dy)
+
+            steps = max(3, args.steps // 2)
+            rr = {"halo_fwd_ms": time_ms(halo_fwd, steps, 2), "map_fwd_ms": time_ms(map_fwd, steps, 2),
+                  "halo_fwd_bwd_ms": time_ms(halo_train, steps, 1), "map_fwd_bwd_ms": time_ms(map_train, steps, 1)}
+            rr["halo_errors_vs_fp64"] = rel_errors(halo_fwd(), y64)
+            rr["map_errors_vs_fp64"] = rel_errors(map_fwd(), y64)
+            res[name] = rr
+        out[gname] = res
+    return out
 
 
 def box_surface_ijk(n_boxes: int, resolution: int, seed: int, device) -> torch.Tensor:
@@ -652,9 +733,10 @@ def leg_fp8(fvdb, dev, args) -> dict:
     FP8 and BF16; errors vs FP64 on 4096 sampled output rows."""
     # sphere shells (seeds 300, 301, ...) are added until their union holds ~4M voxels
     ijk = torch.zeros((0, 3), dtype=torch.int32, device=dev)
+    target = args.c4_voxels
     for i in range(16):
-        ijk = torch.unique(torch.cat([ijk, shell_ijk(1_000_000, 300 + i, dev, 1024)]), dim=0)
-        if ijk.shape[0] >= 4_000_000:
+        ijk = torch.unique(torch.cat([ijk, shell_ijk(min(1_000_000, target), 300 + i, dev, 1024)]), dim=0)
+        if ijk.shape[0] >= target:
             break
     grid = fvdb.GridBatch.from_ijk(ijk)
     g = torch.Generator().manual_seed(301)
@@ -766,13 +848,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / training / FP8 / serving legs")
-    ap.add_argument("--legs", default="fp32,c1,train,fp8,serve",
+    ap.add_argument("--legs", default="fp32,c1,halo,train,fp8,serve",
                     help="comma-separated extra legs to run after the headline step")
     ap.add_argument("--serve-rates", default="50,100,200,500,1000,2000",
                     help="Poisson request rates of the serving sweep (1/s)")
     ap.add_argument("--serve-requests", type=int, default=300, help="requests per rate in the serving leg")
     ap.add_argument("--serve-pool", type=int, default=40, help="distinct request grids the serving leg draws from")
     ap.add_argument("--serve-error-sample", type=int, default=4, help="served requests checked against FP64")
+    ap.add_argument("--c4-voxels", type=int, default=4_000_000,
+                    help="voxels of the FP8 leg's grid (4M is the stated size; smaller only for profiling captures)")
     ap.add_argument("--points", type=int, default=2_000_000,
                     help="points per grid (the headline workload uses 2M; smaller only for profiling captures)")
     args = ap.parse_args()

@@ -2,6 +2,7 @@
 #include <stdio.h>
 
 #include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -19,6 +20,20 @@ int record_cuda(cudaError_t e) {
     if (e == cudaSuccess) return FVGB_OK;
     snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
     return FVGB_ECUDA;
+}
+
+int device_sm_count() {
+    static std::mutex mu;
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+        cache[dev] = n;
+    }
+    return cache[dev];
 }
 
 }  // namespace fvgb

@@ -19,6 +19,8 @@ inline int launch_status() { return record_cuda(cudaGetLastError()); }
 void count_launches(int n);
 
 inline cudaStream_t as_stream(fvgb_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+// Streaming multiprocessors of the current device (cached per device).
+int device_sm_count();
 
 constexpr int kLeafDim = 8;
 // find_leaf reads (origin, batch) of a leaf as one 16-byte load: leaves must stay 128 bytes.

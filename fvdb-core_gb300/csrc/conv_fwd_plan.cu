@@ -721,19 +721,7 @@ int plan_tile_n(int32_t cout) {
     return -1;
 }
 
-int sm_count_p() {
-    static std::mutex mu;
-    static int cache[64] = {0};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!cache[dev]) {
-        int n = 0;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
-        cache[dev] = n;
-    }
-    return cache[dev];
-}
+int sm_count_p() { return device_sm_count(); }
 
 template <int BN, int EB, int PACK>
 int launch_plan(PlanArgs a, cudaStream_t s) {

@@ -555,19 +555,7 @@ int64_t weight_units(int64_t K, int64_t row_bytes, int *pack, int *nchunks) {
     return *pack > 1 ? ceil_div(K, (int64_t)*pack) : K * *nchunks;
 }
 
-int sm_count() {
-    static std::mutex mu;
-    static int cache[64] = {0};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!cache[dev]) {
-        int n = 0;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
-        cache[dev] = n;
-    }
-    return cache[dev];
-}
+int sm_count() { return device_sm_count(); }
 
 template <int BN, int EB, int PACK>
 int launch_fwd(FwdArgs a, cudaStream_t s) {

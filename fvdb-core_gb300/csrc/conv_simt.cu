@@ -1,7 +1,7 @@
 // CUDA-core contractions: the plain FP32 form (no TF32) and the FP64 form.
 //
-// Forward:  y[m,:] (+)= sum_k x[map[m,k],:] . W[k]   (one CTA owns a 64x64 output tile; every
-//           output element is written exactly once, no atomics).  Offsets whose 64 map entries
+// Forward:  y[m,:] (+)= sum_k x[map[m,k],:] . W[k]   (one CTA owns a 128x64 output tile; every
+//           output element is written exactly once, no atomics).  Offsets whose 128 map entries
 //           are all -1 are skipped.  With the transposed map and W^T strides the same kernel is
 //           the data gradient.
 // Wgrad:    dW[k,ci,co] = sum_m x[map[m,k],ci] * dy[m,co] with per-CTA partials and a
@@ -14,8 +14,31 @@
 namespace fvgb {
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;  // wgrad tile
+constexpr int FM = 128, FN = 64;                    // forward tile: 128 rows x 64 channels, 8 x 4 per thread
 
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+    __device__ static void load(const float *p, float (&v)[4]) {
+        const float4 q = *reinterpret_cast<const float4 *>(p);
+        v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+    }
+};
+template <>
+struct Vec4<double> {
+    __device__ static void load(const double *p, double (&v)[4]) {
+        const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+        v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+    }
+};
+
+// One CTA per 128-row x 64-channel output tile, 256 threads of 8 rows x 4 channels.  Per
+// offset with any present row and per 16-channel slice (8 for FP64), the gathered rows (transposed, so a
+// thread's 8 rows are two vector loads) and the weight slice go through shared memory; the
+// slice after is loaded into registers while this one is multiplied, so one barrier per slice
+// separates the two shared-memory buffers.
 template <typename T>
 __global__ void __launch_bounds__(NT) conv_fwd_simt_kernel(const T *__restrict__ x, int64_t n_x, int32_t cin,
                                                            int64_t ldx, const int32_t *__restrict__ map,
@@ -23,60 +46,109 @@ __global__ void __launch_bounds__(NT) conv_fwd_simt_kernel(const T *__restrict__
                                                            const T *__restrict__ w, int64_t wsk, int64_t wsci,
                                                            int64_t wsco, T *__restrict__ y, int32_t cout,
                                                            int64_t ldy, int32_t accumulate) {
-    __shared__ int32_t rows[BM];
-    __shared__ T As[BK][BM + 4];
-    __shared__ T Bs[BK][BN + 4];
+    constexpr int FK = sizeof(T) == 8 ? 8 : 16;  // channels per slice (static shared memory < 48 KB)
+    constexpr int QA = FM * FK / NT, QB = FK * FN / NT;
+    __shared__ int32_t rows[2][FM];
+    __shared__ __align__(16) T As[2][FK][FM + 4];
+    __shared__ __align__(16) T Bs[2][FK][FN + 4];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int64_t m0 = (int64_t)blockIdx.x * BM;
-    const int32_t n0 = blockIdx.y * BN;
-    T acc[4][4];
+    const int64_t m0 = (int64_t)blockIdx.x * FM;
+    const int32_t n0 = blockIdx.y * FN;
+    T acc[8][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
 
-    for (int32_t k = 0; k < K; ++k) {
+    // rows of offset k into rows[rb]; true if any is present (a CTA-wide vote)
+    auto load_rows = [&](int32_t k, int rb) -> bool {
         int valid = 0;
-        if (tid < BM) {
+        if (tid < FM) {
             const int64_t r = m0 + tid;
             int32_t v = r < n_out ? map[r * ldm + k] : -1;
             if (v >= n_x) v = -1;
-            rows[tid] = v;
+            rows[rb][tid] = v;
             valid = v >= 0;
         }
-        if (!__syncthreads_or(valid)) continue;
-        for (int32_t c0 = 0; c0 < cin; c0 += BK) {
+        return __syncthreads_or(valid) != 0;
+    };
+    // per thread: A elements e = tid + 256 q (q < QA) -> (row e / FK, channel e % FK); B elements
+    // e = tid + 256 q (q < QB) -> (channel e / 64, column e % 64)
+    T ra[QA], rb4[QB];
+    auto fetch = [&](int32_t k, int32_t c0, int rbuf) {
 #pragma unroll
-            for (int q = 0; q < (BM * BK) / NT; ++q) {
-                const int e = tid + q * NT, r = e / BK, c = e % BK;
-                const int32_t src = rows[r];
-                As[c][r] = (src >= 0 && c0 + c < cin) ? x[(int64_t)src * ldx + c0 + c] : T(0);
-            }
+        for (int q = 0; q < QA; ++q) {
+            const int e = tid + q * NT, r = e / FK, c = e % FK;
+            const int32_t src = rows[rbuf][r];
+            ra[q] = (src >= 0 && c0 + c < cin) ? x[(int64_t)src * ldx + c0 + c] : T(0);
+        }
 #pragma unroll
-            for (int q = 0; q < (BK * BN) / NT; ++q) {
-                const int e = tid + q * NT, c = e / BN, n = e % BN;
-                Bs[c][n] = (c0 + c < cin && n0 + n < cout) ? w[k * wsk + (int64_t)(c0 + c) * wsci + (int64_t)(n0 + n) * wsco]
-                                                           : T(0);
+        for (int q = 0; q < QB; ++q) {
+            const int e = tid + q * NT, c = e >> 6, n = e & 63;
+            rb4[q] = (c0 + c < cin && n0 + n < cout)
+                         ? w[k * wsk + (int64_t)(c0 + c) * wsci + (int64_t)(n0 + n) * wsco]
+                         : T(0);
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < QA; ++q) {
+            const int e = tid + q * NT;
+            As[buf][e % FK][e / FK] = ra[q];
+        }
+#pragma unroll
+        for (int q = 0; q < QB; ++q) {
+            const int e = tid + q * NT;
+            Bs[buf][e >> 6][e & 63] = rb4[q];
+        }
+    };
+
+    // walk (offset, channel slice) pairs, skipping offsets with no present row
+    int32_t k = 0;
+    int rbuf = 0;
+    while (k < K && !load_rows(k, rbuf)) ++k;
+    if (k < K) {
+        int32_t c0 = 0;
+        fetch(k, c0, rbuf);
+        store(0);
+        __syncthreads();
+        int buf = 0;
+        while (true) {
+            // the next (offset, slice)
+            int32_t kn = k, cn = c0 + FK;
+            int rn = rbuf;
+            if (cn >= cin) {
+                cn = 0;
+                rn = rbuf ^ 1;
+                ++kn;
+                while (kn < K && !load_rows(kn, rn)) ++kn;
             }
+            const bool more = kn < K;
+            if (more) fetch(kn, cn, rn);
+#pragma unroll
+            for (int c = 0; c < FK; ++c) {
+                T a[8], b[4];
+                T a0[4], a1[4];
+                Vec4<T>::load(&As[buf][c][ty * 8], a0);
+                Vec4<T>::load(&As[buf][c][ty * 8 + 4], a1);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) a[i] = a0[i], a[i + 4] = a1[i];
+                Vec4<T>::load(&Bs[buf][c][tx * 4], b);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+            }
+            if (!more) break;
+            store(buf ^ 1);
             __syncthreads();
-#pragma unroll
-            for (int c = 0; c < BK; ++c) {
-                T a[4], bb[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) a[i] = As[c][ty * 4 + i];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) bb[j] = Bs[c][tx * 4 + j];
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
-            }
-            __syncthreads();
+            buf ^= 1;
+            k = kn, c0 = cn, rbuf = rn;
         }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int64_t r = m0 + ty * 4 + i;
+    for (int i = 0; i < 8; ++i) {
+        const int64_t r = m0 + ty * 8 + i;
         if (r >= n_out) continue;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -199,7 +271,7 @@ extern "C" int fvgb_conv_fwd_simt(int32_t dtype, const void *x, int64_t n_x, int
         return FVGB_EINVAL;
     if (n_out == 0) return FVGB_OK;
     if (!map || !w || !y || (n_x > 0 && !x)) return FVGB_EINVAL;
-    const dim3 grid((unsigned)ceil_div(n_out, BM), (unsigned)ceil_div(c_out, BN));
+    const dim3 grid((unsigned)ceil_div(n_out, FM), (unsigned)ceil_div(c_out, FN));
     if (grid.y > 65535) return FVGB_EINVAL;
     cudaStream_t s = as_stream(stream);
     if (dtype == FVGB_F32) {
@@ -363,5 +435,37 @@ extern "C" int fvgb_conv_wgrad_simt_noalloc(int32_t dtype, const void *x, int64_
             part, n_out > 0 ? p.chunks : 0, per_chunk, (double *)dw);
     }
     count_launches(n_out > 0 ? 2 : 1);
+    return launch_status();
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP32 FMA rate probe: every thread runs 8 independent fma chains of `iters` steps (enough
+// independent work to keep the FMA pipes full), 2 * 8 * iters FLOPs per thread.  The caller
+// times the launch; the chains' sum is written so that nothing is optimised away.
+namespace fvgb {
+namespace {
+__global__ void __launch_bounds__(256) ffma_probe_kernel(float *out, int64_t iters, float b, float c) {
+    float v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = (float)(threadIdx.x + i);
+    for (int64_t it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) v[i] = fmaf(v[i], b, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += v[i];
+    if (s == 12345.678f) out[0] = s;  // practically never true: keeps the chains live
+    if (threadIdx.x == 0 && blockIdx.x == 0) out[1] = s;
+}
+}  // namespace
+}  // namespace fvgb
+
+extern "C" int fvgb_ffma_probe(float *out, int64_t iters, int32_t blocks_per_sm, double *flops, fvgb_stream_t stream) {
+    if (!out || iters < 1 || blocks_per_sm < 1 || blocks_per_sm > 64 || !flops) return FVGB_EINVAL;
+    const int64_t blocks = (int64_t)device_sm_count() * blocks_per_sm;
+    ffma_probe_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(out, iters, 0.999999f, 1e-7f);
+    *flops = 2.0 * 8.0 * (double)iters * 256.0 * (double)blocks;
+    count_launches(1);
     return launch_status();
 }

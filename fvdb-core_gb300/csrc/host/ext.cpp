@@ -977,6 +977,48 @@ Tensor pool_backward(int32_t mode, const GridPtr &fine, const GridPtr &coarse, c
     return dx.reshape(x.sizes());
 }
 
+// Stride-1 3^3 convolution over the grid without a kernel map: y = sum_k x[v + d_k] W[k] for
+// W [27, Cin, Cout] (mirror: the data gradient, W[26-k]^T with W in the forward's layout).
+Tensor halo_conv(const GridPtr &g, const Tensor &x, const Tensor &w, bool mirror) {
+    c10::cuda::CUDAGuard guard(g->device());
+    TORCH_CHECK_VALUE(x.dim() == 2 && x.size(0) == g->N, "features must have shape (num_voxels, channels)");
+    TORCH_CHECK_VALUE(w.dim() == 3 && w.size(0) == 27, "halo weights must have shape (27, in, out)");
+    TORCH_CHECK_TYPE(w.scalar_type() == x.scalar_type(), "halo weights and features must have the same dtype");
+    const int64_t cin = x.size(1), cout = mirror ? w.size(1) : w.size(2);
+    TORCH_CHECK_VALUE((mirror ? w.size(2) : w.size(1)) == cin, "halo weights do not match the feature channels");
+    Tensor xc = x.contiguous(), wc = w.contiguous();
+    Tensor y = torch::empty({g->N, cout}, x.options());
+    if (g->N > 0 && cin > 0 && cout > 0) {
+        FvgbGrid v = g->view();
+        check_status(fvgb_halo_conv(fvgb_dtype(x), &v, xc.data_ptr(), cin, (int32_t)cin, wc.data_ptr(), (int32_t)cout,
+                                    mirror ? 1 : 0, y.data_ptr(), cout, cur_stream()),
+                     "halo convolution");
+    } else if (cout > 0) {
+        y.zero_();
+    }
+    return y;
+}
+
+// dW [27, Cin, Cout] = sum_v x[v + d_k]^T dy[v] (fixed-order FP64 sum of per-chunk partials)
+Tensor halo_wgrad(const GridPtr &g, const Tensor &x, const Tensor &dy) {
+    c10::cuda::CUDAGuard guard(g->device());
+    TORCH_CHECK_VALUE(x.dim() == 2 && dy.dim() == 2 && x.size(0) == g->N && dy.size(0) == g->N,
+                      "features and gradients must have shape (num_voxels, channels)");
+    Tensor xc = x.contiguous(), dc = dy.to(x.scalar_type()).contiguous();
+    const int64_t cin = x.size(1), cout = dy.size(1);
+    Tensor dw = torch::empty({27, cin, cout}, x.options());
+    if (cin == 0 || cout == 0) return dw;
+    FvgbGrid v = g->view();
+    size_t wsb = 0;
+    check_status(fvgb_halo_wgrad_workspace(fvgb_dtype(x), &v, (int32_t)cin, (int32_t)cout, &wsb), "halo wgrad workspace");
+    Tensor ws = workspace(wsb, x.device());
+    check_status(fvgb_halo_wgrad(fvgb_dtype(x), &v, g->N ? xc.data_ptr() : nullptr, cin, (int32_t)cin,
+                                 g->N ? dc.data_ptr() : nullptr, cout, (int32_t)cout, dw.data_ptr(), ws.data_ptr(),
+                                 ws.numel(), cur_stream()),
+                 "halo weight gradient");
+    return dw;
+}
+
 // y [fine N, *] = nearest upsampling of x [coarse N, *]
 Tensor upsample_forward(const GridPtr &coarse, const GridPtr &fine, const std::vector<int64_t> &factor, const Tensor &x) {
     c10::cuda::CUDAGuard guard(fine->device());
@@ -1086,6 +1128,8 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); },
           py::call_guard<py::gil_scoped_release>());
     m.def("conv_backward", &conv_backward, py::call_guard<py::gil_scoped_release>());
+    m.def("halo_conv", &halo_conv, py::call_guard<py::gil_scoped_release>());
+    m.def("halo_wgrad", &halo_wgrad, py::call_guard<py::gil_scoped_release>());
     m.def("pool_forward", &pool_forward);
     m.def("pool_backward", &pool_backward);
     m.def("upsample_forward", &upsample_forward);

@@ -88,7 +88,6 @@ def _mask_data(mask, grid) -> torch.Tensor | None:
 class GridBatch:
     def __init__(self, *, impl):
         self._impl = impl
-        self._halo_pack = None  # stride-1 3^3 kernel map for sparse_conv_halo, built on first use
 
     # ---------------------------------------------------------------- constructors -------
     @classmethod
@@ -166,11 +165,12 @@ class GridBatch:
     def sparse_conv_halo(self, input: JaggedTensor, weight: torch.Tensor, variant: int = 8) -> JaggedTensor:
         """Stride-1 3x3x3 convolution of `input` (one feature row per voxel) over this grid, with
         the reference's arguments, checks and error types (GridBatch.cpp:776-793,
-        autograd/SparseConvolutionHalo.cpp:17-86).  The reference computes it from a 10^3 halo
-        per leaf whose x, y, z offsets meet weight dims 4, 3, 2 (K2, K1, K0): the kernel map's
-        convention, so the result is sparse_conv_3d over the grid's stride-1 3^3 map, with the
-        same data and weight gradients.  `variant` picks one of the reference's halo kernels and
-        is accepted for compatibility (there is one implementation)."""
+        autograd/SparseConvolutionHalo.cpp:17-86).  Computed without a kernel map: a CTA per
+        leaf stages the leaf's 10^3 halo (through the leaf hash) in shared memory and convolves
+        its active voxels; x, y, z offsets meet weight dims 4, 3, 2 (K2, K1, K0), the kernel
+        map's convention, so the result equals sparse_conv_3d over the grid's stride-1 3^3 map
+        up to summation order.  `variant` picks one of the reference's halo kernels and is
+        accepted for compatibility (there is one implementation)."""
         if not isinstance(input, JaggedTensor):
             raise TypeError("input must be a JaggedTensor")
         data = input.jdata
@@ -194,9 +194,9 @@ class GridBatch:
         if weight.shape[1] != data.shape[1]:
             raise ValueError(f"Expected input channels of kernels ({weight.shape[1]}) to equal input channels of "
                              f"features: {data.shape[1]}")
-        if self._halo_pack is None:
-            self._halo_pack, _ = self.sparse_conv_kernel_map(3, 1)
-        return input.jagged_like(self._halo_pack.sparse_conv_3d(data, weight).jdata)
+        from ._halo import HaloConvFunction
+
+        return input.jagged_like(HaloConvFunction.apply(self._impl, data, weight))
 
     # ---------------------------------------------------------------- pooling -----------
     def coarsened_grid(self, coarsening_factor: Numeric) -> "GridBatch":

@@ -371,9 +371,12 @@ int fvgb_conv_fwd_tc_planned(int32_t dtype, const void *x, int64_t n_x, int32_t 
 /*
  * Tensor-core weight gradient, BF16 operands:  dw[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co]
  * (FP32, [K, c_in, c_out] contiguous).  c_in in {32, 64, 128} (128/c_in offsets share one
- * M=128 MMA), c_out in {64, 128, 256}; rows of x and dy 16-byte aligned.  Per-CTA FP32
- * partials go to `workspace` (fvgb_tc_wgrad_workspace bytes) and are summed across CTAs in
- * FP64 in a fixed order (deterministic).  tile_mask as for fvgb_conv_fwd_tc (may be null).
+ * M=128 MMA), c_out in {64, 128, 256}; rows of x and dy 16-byte aligned; map as for
+ * fvgb_conv_fwd_tc ([ceil(n_out/128)*128, K], padding rows -1, 16-byte aligned).  dy is read
+ * with TMA tile loads (a tensor map is encoded per call).  Per-CTA FP32 partials go to
+ * `workspace` (fvgb_tc_wgrad_workspace bytes, which depend on the device's SM count) and are
+ * summed across CTAs in FP64 in a fixed order (deterministic).  tile_mask as for
+ * fvgb_conv_fwd_tc (may be null).
  * Replaces the split-K implicit-GEMM wgrad
  * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionImplicitGEMMGrad.cu:115-4101,
  *  SparseConvolutionImplicitGEMMGradSorted.cu:115-4582).
@@ -442,6 +445,34 @@ int fvgb_upsample_backward(int32_t dtype, const FvgbGrid *coarse, const FvgbGrid
  * (src/fvdb/detail/ops/BuildFineGridFromCoarse.cu:66-226,343-352). */
 int fvgb_subdivide_candidates(const FvgbGrid *coarse, const int32_t factor[3], const uint8_t *mask, int32_t *out_ijk,
                               uint8_t *out_valid, fvgb_stream_t stream);
+
+/* FP32 FMA rate probe (for reporting the CUDA-core roofline of the plain FP32 form): launches
+ * blocks_per_sm x SMs CTAs of 256 threads, each thread 8 independent fma chains of `iters` steps;
+ * *flops (host) = FLOPs of the launch, which the caller times on `stream`.  out: device float[2].
+ * No counterpart in the reference. */
+int fvgb_ffma_probe(float *out, int64_t iters, int32_t blocks_per_sm, double *flops, fvgb_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Leaf-halo convolution: stride-1 3x3x3 convolution of a grid onto itself with no kernel map.
+ * Offset k = 9*a + 3*b + c reads the voxel at ijk + (a-1, b-1, c-1) (the kernel map's order,
+ * weight dims K2, K1, K0 on ijk axes 0, 1, 2).  dtype FVGB_F32 / FVGB_F64 / FVGB_BF16 / FVGB_F16,
+ * FP32 accumulation (FP64 for FP64), CUDA cores.
+ * ------------------------------------------------------------------------------------------ */
+/* y [n, c_out] = sum_k x[v + d_k] . w[k], w [27, c_in, c_out].  mirror != 0: the data gradient,
+ * offset k takes w[26-k]^T with w in the forward layout [27, c_out, c_in] (x = dy, y = dx).
+ * Replaces stencilConvHaloKernel and the dgrad of its backward
+ * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionHalo.cu:22-351,
+ * src/fvdb/detail/autograd/SparseConvolutionHalo.cpp:17-86). */
+int fvgb_halo_conv(int32_t dtype, const FvgbGrid *grid, const void *x, int64_t ldx, int32_t c_in, const void *w,
+                   int32_t c_out, int32_t mirror, void *y, int64_t ldy, fvgb_stream_t stream);
+/* Workspace bytes of fvgb_halo_wgrad. */
+int fvgb_halo_wgrad_workspace(int32_t dtype, const FvgbGrid *grid, int32_t c_in, int32_t c_out, size_t *bytes);
+/* dw [27, c_in, c_out] = sum_v x[v + d_k]^T dy[v]: per-chunk partials summed in FP64 in a fixed
+ * order (deterministic).  Replaces the halo weight gradient
+ * (src/fvdb/detail/ops/convolution/backend/SparseConvolutionHaloGrad.cu:161-273). */
+int fvgb_halo_wgrad(int32_t dtype, const FvgbGrid *grid, const void *x, int64_t ldx, int32_t c_in, const void *dy,
+                    int64_t lddy, int32_t c_out, void *dw, void *workspace, size_t workspace_bytes,
+                    fvgb_stream_t stream);
 
 #ifdef __cplusplus
 }

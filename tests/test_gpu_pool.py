@@ -112,8 +112,9 @@ def test_upsample_bit_exact(fvdb, cuda_device, dtype, factor, masked):
     assert np.array_equal(xd.grad.cpu().numpy(), orc.upsample_backward(ijk, off, f, foff_o, dy.numpy(), factor))
     # fine transform as the reference: size w/f, origin o - (f-1) w / (2f)
     fv = torch.tensor(orc._vec3(factor), dtype=torch.float64)
-    assert torch.allclose(fg.voxel_sizes[0], g.voxel_sizes[0] / fv)
-    assert torch.allclose(fg.origins[0], g.origins[0] - (fv - 1) * g.voxel_sizes[0] / fv * 0.5)
+    vs, org = g.voxel_sizes[0].cpu().double(), g.origins[0].cpu().double()
+    assert torch.allclose(fg.voxel_sizes[0].cpu().double(), vs / fv)
+    assert torch.allclose(fg.origins[0].cpu().double(), org - (fv - 1) * vs / fv * 0.5)
 
 
 def test_upsample_module_onto_user_grid(fvdb, cuda_device):

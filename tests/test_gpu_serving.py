@@ -60,3 +60,23 @@ def test_oversized_request_rejected_on_gpu(cuda_device):
     out = {r.rid: r for r in srv.serve([big, small])}
     assert out[0].error is not None
     assert out[1].error is None and out[1].output.shape == (500, 64)
+
+
+def test_footprint_bounds_measured_peak(cuda_device):
+    """Admission's footprint() (the sum over a batch's requests) bounds the device memory the
+    batch really takes: the growth of torch's peak allocation while the batch runs."""
+    from fvdb.serving import ConvStack, GPUExecutor
+
+    model = ConvStack([32, 64, 64, 32], cuda_device, seed=0)
+    ex = GPUExecutor(model, cuda_device, slots=1)
+    for seed, n_req in ((2, 1), (3, 6)):
+        batch = _requests(n_req, seed)
+        ex._run(batch, 0)  # first call: weight images and library state
+        torch.cuda.synchronize(cuda_device)
+        base = torch.cuda.memory_allocated(cuda_device)
+        torch.cuda.reset_peak_memory_stats(cuda_device)
+        ev, *_ = ex._run(batch, 0)
+        ev.synchronize()
+        peak = torch.cuda.max_memory_allocated(cuda_device) - base
+        need = sum(ex.footprint(r) for r in batch)
+        assert peak <= need, f"batch of {sum(r.n_voxels for r in batch)} voxels peaked at {peak} B > footprint {need} B"
