@@ -157,12 +157,12 @@ L1_DRAM_BYTES_PER_VOXEL = (142.949e6 + 70.459e6) / 829_865
 
 
 def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) -> dict:
-    """Layer-1 tcgen05 contraction alone through the C ABI: the planned kernel
-    (fvgb_conv_fwd_tc_planned over the pack's tile plan, the one the step runs) and, for
-    comparison, the unplanned kernel (fvgb_conv_fwd_tc over the int32 map).  Average launch
-    durations from CUDA events around `launches` back-to-back launches on the current stream,
-    and whether each output is bitwise identical to the same layer run through
-    SparseConvPackInfo.sparse_conv_3d."""
+    """Layer-1 tcgen05 contraction alone through the C ABI: over the index order (fvgb_conv_fwd_tc --
+    the kernel the step runs) and, for comparison, over the map's row order (rows sorted by
+    occupancy mask, fvgb_conv_fwd_tc_rows) and over a tile plan (fvgb_conv_fwd_tc_planned); plus
+    the cost of building the row order and the plan.  Average launch durations from CUDA events
+    around `launches` back-to-back launches on the current stream, and whether each output is
+    bitwise identical to the same layer run through SparseConvPackInfo.sparse_conv_3d."""
     import ctypes
 
     n = x.shape[0]
@@ -180,7 +180,25 @@ def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) ->
     assert lib.fvgb_tc_pack_weights(2, P(wkio), ctypes.c_int64(K), cin, cout, ctypes.c_int64(cin * cout),
                                     ctypes.c_int64(cout), ctypes.c_int64(1), P(packed), nb, stream) == 0
     err = torch.zeros(1, dtype=torch.int32, device=x.device)
+    tiles = (n + 127) // 128
+    rows = torch.empty(tiles * 128, dtype=torch.int32, device=x.device)
+    rmask = torch.zeros(tiles, dtype=torch.int32, device=x.device)
+    smap = torch.empty(tiles * 128, K, dtype=torch.int32, device=x.device)
+    wsb = ctypes.c_size_t(0)
+    assert lib.fvgb_kmap_row_order_workspace(ctypes.c_int64(n), K, ctypes.byref(wsb)) == 0
+    ws = torch.empty(wsb.value, dtype=torch.uint8, device=x.device)
     ref = p1.sparse_conv_3d(x, w1).jdata
+
+    def build_order(_y):
+        rc = lib.fvgb_kmap_row_order(P(kmap), ctypes.c_int64(n), K, ctypes.c_int64(K), P(rows), P(rmask), P(smap),
+                                     P(ws), ctypes.c_size_t(ws.numel()), stream)
+        assert rc == 0, rc
+
+    def ordered(y):
+        rc = lib.fvgb_conv_fwd_tc_rows(2, P(x), ctypes.c_int64(n), cin, ctypes.c_int64(x.stride(0)), P(smap),
+                                       ctypes.c_int64(n), K, P(rows), P(rmask), P(packed), cout, P(y),
+                                       ctypes.c_int64(cout), None, None, 0, P(err), stream)
+        assert rc == 0, rc
 
     def planned(y):
         rc = lib.fvgb_conv_fwd_tc_planned(2, P(x), ctypes.c_int64(n), cin, ctypes.c_int64(x.stride(0)), P(plan),
@@ -199,8 +217,10 @@ def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) ->
                                     stream)
         assert rc == 0, rc
 
+    build_order(None)
     out = {}
-    for name, fn in (("planned", planned), ("unplanned", unplanned), ("plan_build", build_plan)):
+    for name, fn in (("ordered", ordered), ("planned", planned), ("unplanned", unplanned), ("plan_build", build_plan),
+                     ("order_build", build_order)):
         y = torch.empty(n, cout, device=x.device, dtype=torch.bfloat16)
         fn(y)
         torch.cuda.synchronize()
@@ -212,7 +232,7 @@ def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) ->
         torch.cuda.synchronize()
         assert int(err.item()) == 0
         out[name] = {"ms": a.elapsed_time(b) / launches, "identical_to_step": bool(torch.equal(ref, y))}
-    del out["plan_build"]["identical_to_step"]
+    del out["plan_build"]["identical_to_step"], out["order_build"]["identical_to_step"]
     return out
 
 
@@ -393,8 +413,8 @@ def run_gpu(args) -> None:
         e2e_ms = t0.elapsed_time(t1) / e2e_steps
 
     kern = kernel_only_l1(lib, p1, x, model.w1, max(args.steps, 3))
-    # the step builds its kernel maps every step, so it runs the unplanned kernel (a tile plan is
-    # built only for a map that is used again); the planned kernel is timed beside it
+    # the step builds its kernel maps every step, so it runs the index-order kernel (a row order or
+    # a tile plan is built only for a map that is used again); the others are timed beside it
     kern_ms, kern_identical = kern["unplanned"]["ms"], kern["unplanned"]["identical_to_step"]
     peaks = load_peaks()
     conv1_flops = 2.0 * P1 * 32 * 64
@@ -435,6 +455,9 @@ def run_gpu(args) -> None:
             "kernel_tflops": conv1_flops / (kern_ms * 1e-3) / 1e12,
             "tensor_frac": conv1_flops / (kern_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
             "layer1_window_ms": conv_ms,
+            "row_order_build_ms": kern["order_build"]["ms"],
+            "row_order_kernel_ms": kern["ordered"]["ms"],
+            "row_order_output_identical_to_step": kern["ordered"]["identical_to_step"],
             "planned_kernel_ms": kern["planned"]["ms"],
             "planned_output_identical_to_step": kern["planned"]["identical_to_step"],
             "plan_build_ms": kern["plan_build"]["ms"],

@@ -89,6 +89,7 @@ struct FwdArgs {
     int32_t stages;
     int64_t n_tiles;
     int32_t direct_store;  // 1: output rows contiguous (ldy == cout, cout % 8 == 0): one bulk store per tile
+    const int32_t *out_rows;  // null: map row m computes output row m; else output row out_rows[m] (-1 = none)
 };
 
 // Active units of one tile: a bit set (K <= 32 with a mask) or all units in order.
@@ -386,8 +387,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
             const int64_t left = a.n_out - m0;
             const int rows = left < kTileM ? (int)left : kTileM;
             const uint32_t tbase = tmem + b * BN + ((uint32_t)(q4 * 32) << 16);
+            // the output row this thread drains (rows of a given order: one bulk store per row)
+            const int64_t yrow_i = rt >= rows ? -1 : (a.out_rows ? (int64_t)__ldg(a.out_rows + m0 + rt) : m0 + rt);
             if (a.direct_store) {
-                if (et == 0) bulk_wait_read<0>();  // the staging tile of the previous store has been read
+                // the staging tile of the previous store has been read
+                if (a.out_rows || et == 0) bulk_wait_read<0>();
                 named_barrier(1, kTileM);
             }
 #pragma unroll 1
@@ -426,7 +430,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
                     dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
                     if (c0 + 8 < a.cout) dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
                 } else {
-                    __nv_bfloat16 *yrow = reinterpret_cast<__nv_bfloat16 *>(a.y) + (m0 + rt) * a.ldy;
+                    __nv_bfloat16 *yrow = reinterpret_cast<__nv_bfloat16 *>(a.y) + yrow_i * a.ldy;
 #pragma unroll
                     for (int t = 0; t < 8; ++t) {
                         const __nv_bfloat162 h2 = *reinterpret_cast<const __nv_bfloat162 *>(&packed[t]);
@@ -441,13 +445,19 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tc_fwd_kernel(FwdArgs a) {
             if (a.direct_store) {
                 fence_proxy_async();  // staging writes -> visible to the bulk store (async proxy)
                 named_barrier(1, kTileM);
-                if (et == 0) {
+                if (a.out_rows) {
+                    if (yrow_i >= 0) {
+                        bulk_s2g(a.y + yrow_i * a.ldy * 2, smem_u32(ystage + (size_t)rt * a.cout * 2),
+                                 (uint32_t)(a.cout * 2));
+                        bulk_commit();
+                    }
+                } else if (et == 0) {
                     bulk_s2g(a.y + m0 * a.ldy * 2, smem_u32(ystage), (uint32_t)(rows * a.cout * 2));
                     bulk_commit();
                 }
             }
         }
-        if (a.direct_store && et == 0) bulk_wait<0>();
+        if (a.direct_store && (a.out_rows || et == 0)) bulk_wait<0>();
     } else {
         // ----------------------------------------------------------------- loader (bulk copies)
         if (lane == 0) {
@@ -660,6 +670,15 @@ extern "C" int fvgb_conv_fwd_tc_epilogue(int32_t dtype, const void *x, int64_t n
                                          const void *packed_w, int32_t c_out, void *y, int64_t ldy,
                                          const float *out_scale, const float *bias, int32_t relu, int32_t *err_dev,
                                          fvgb_stream_t stream) {
+    return fvgb_conv_fwd_tc_rows(dtype, x, n_x, c_in, ldx, map, n_out, K, nullptr, tile_mask, packed_w, c_out, y, ldy,
+                                 out_scale, bias, relu, err_dev, stream);
+}
+
+extern "C" int fvgb_conv_fwd_tc_rows(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                     const int32_t *map, int64_t n_out, int32_t K, const int32_t *rows,
+                                     const uint32_t *tile_mask, const void *packed_w, int32_t c_out, void *y,
+                                     int64_t ldy, const float *out_scale, const float *bias, int32_t relu,
+                                     int32_t *err_dev, fvgb_stream_t stream) {
     const int eb = dtype == FVGB_E4M3 ? 1 : (dtype == FVGB_BF16 ? 2 : 0);
     if (!eb) return FVGB_ETYPE;
     if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldx < c_in || ldy < c_out || !err_dev)
@@ -674,6 +693,7 @@ extern "C" int fvgb_conv_fwd_tc_epilogue(int32_t dtype, const void *x, int64_t n
     if (((uintptr_t)x & 15) || ((uintptr_t)packed_w & 15) || ((uintptr_t)y & 15) || ((uintptr_t)map & 15))
         return FVGB_EINVAL;
     FwdArgs a;
+    a.out_rows = rows;
     // with no input rows every map entry is -1 and nothing is read; keep a valid address anyway
     a.x = (const uint8_t *)(n_x > 0 ? x : y);
     a.n_x = n_x;

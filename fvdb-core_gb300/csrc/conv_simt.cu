@@ -45,7 +45,9 @@ __global__ void __launch_bounds__(NT) conv_fwd_simt_kernel(const T *__restrict__
                                                            int64_t n_out, int32_t K, int64_t ldm,
                                                            const T *__restrict__ w, int64_t wsk, int64_t wsci,
                                                            int64_t wsco, T *__restrict__ y, int32_t cout,
-                                                           int64_t ldy, int32_t accumulate) {
+                                                           int64_t ldy, int32_t accumulate,
+                                                           const int32_t *__restrict__ out_rows) {
+    // map row m (m < n_out) computes output row out_rows[m] (m itself when out_rows is null)
     constexpr int FK = sizeof(T) == 8 ? 8 : 16;  // channels per slice (static shared memory < 48 KB)
     constexpr int QA = FM * FK / NT, QB = FK * FN / NT;
     __shared__ int32_t rows[2][FM];
@@ -148,8 +150,9 @@ __global__ void __launch_bounds__(NT) conv_fwd_simt_kernel(const T *__restrict__
     }
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const int64_t r = m0 + ty * 8 + i;
-        if (r >= n_out) continue;
+        const int64_t t = m0 + ty * 8 + i;
+        if (t >= n_out) continue;
+        const int64_t r = out_rows ? (int64_t)out_rows[t] : t;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int32_t n = n0 + tx * 4 + j;
@@ -267,6 +270,14 @@ extern "C" int fvgb_conv_fwd_simt(int32_t dtype, const void *x, int64_t n_x, int
                                   const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *w,
                                   int64_t wsk, int64_t wsci, int64_t wsco, void *y, int32_t c_out, int64_t ldy,
                                   int32_t accumulate, fvgb_stream_t stream) {
+    return fvgb_conv_fwd_simt_rows(dtype, x, n_x, c_in, ldx, map, n_out, K, ldm, nullptr, w, wsk, wsci, wsco, y, c_out,
+                                   ldy, accumulate, stream);
+}
+
+extern "C" int fvgb_conv_fwd_simt_rows(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx,
+                                       const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const int32_t *rows,
+                                       const void *w, int64_t wsk, int64_t wsci, int64_t wsco, void *y, int32_t c_out,
+                                       int64_t ldy, int32_t accumulate, fvgb_stream_t stream) {
     if (c_in < 1 || c_out < 1 || K < 1 || n_out < 0 || n_x < 0 || ldm < K || ldx < c_in || ldy < c_out)
         return FVGB_EINVAL;
     if (n_out == 0) return FVGB_OK;
@@ -277,11 +288,11 @@ extern "C" int fvgb_conv_fwd_simt(int32_t dtype, const void *x, int64_t n_x, int
     if (dtype == FVGB_F32) {
         conv_fwd_simt_kernel<float><<<grid, NT, 0, s>>>((const float *)x, n_x, c_in, ldx, map, n_out, K, ldm,
                                                         (const float *)w, wsk, wsci, wsco, (float *)y, c_out, ldy,
-                                                        accumulate);
+                                                        accumulate, rows);
     } else if (dtype == FVGB_F64) {
         conv_fwd_simt_kernel<double><<<grid, NT, 0, s>>>((const double *)x, n_x, c_in, ldx, map, n_out, K, ldm,
                                                          (const double *)w, wsk, wsci, wsco, (double *)y, c_out,
-                                                         ldy, accumulate);
+                                                         ldy, accumulate, rows);
     } else {
         return FVGB_ETYPE;
     }

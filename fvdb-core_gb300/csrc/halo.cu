@@ -28,7 +28,7 @@ namespace {
 
 constexpr int kHT = 256;     // threads per CTA
 constexpr int kHalo = 1000;  // 10^3 halo positions
-constexpr int kCoTile = 16;  // output channels per pass (4 groups of 4)
+constexpr int kCoTile = 16;  // output channels per pass (two halves of 8)
 
 template <typename T>
 struct HNum;
@@ -64,8 +64,8 @@ struct HNum<__half> {
 template <typename T>
 constexpr int halo_smem_bytes() {
     using A = typename HNum<T>::A;
-    return kHalo * (HNum<T>::CC + 1) * (int)sizeof(A) + 27 * HNum<T>::CC * kCoTile * (int)sizeof(A) + kHalo * 2 * 4 +
-           512 * 2 * 4 + 48 * 4;
+    return (kHalo + 1) * (HNum<T>::CC + 1) * (int)sizeof(A) + 27 * HNum<T>::CC * kCoTile * (int)sizeof(A) +
+           kHalo * 2 * 4 + 512 * 2 * 4 + 48 * 4;
 }
 
 // Halo of leaf `lf`: the active positions among its 1000 (the leaf and a one-voxel shell of its
@@ -129,46 +129,72 @@ __device__ int2 halo_setup(const FvgbGrid &g, int64_t lf, int32_t *hslot, int32_
     return make_int2(n, n_halo);
 }
 
+template <typename A>
+__device__ __forceinline__ void load8(const A *p, A (&v)[8]);
+template <>
+__device__ __forceinline__ void load8<float>(const float *p, float (&v)[8]) {
+    const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+}
+template <>
+__device__ __forceinline__ void load8<double>(const double *p, double (&v)[8]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const double2 q = reinterpret_cast<const double2 *>(p)[i];
+        v[2 * i] = q.x, v[2 * i + 1] = q.y;
+    }
+}
+
 // y = conv(x, W) over the leaves, W [27, Cin, Cout].  mirror != 0 computes the data gradient:
 // offset k takes W[26-k]^T, with W given as the forward's [27, Cout_fwd = Cin, Cin_fwd = Cout].
-// Per leaf and 16-channel output tile, the CTA loops over input-channel chunks of CC: the chunk's
-// rows of the active halo positions and its 27 x CC x 16 weights are staged in shared memory
-// (zero-padded channels), then thread item i = (voxel i / 4, output group i % 4) accumulates 4
-// output channels.
+// Per leaf and 16-channel output tile, the CTA loops over input-channel slices of CC: the slice's
+// rows of the active halo positions (plus one zero row that absent positions read) and its
+// 27 x CC x 16 weights are staged in shared memory (zero-padded channels); thread t accumulates
+// 4 active voxels (4 (t/2) ..) x 8 output channels (8 (t%2) ..), so every staged value it loads
+// feeds 4 or 8 FMAs.
 template <typename T>
-__global__ void __launch_bounds__(kHT) halo_fwd_kernel(FvgbGrid g, const T *__restrict__ x, int64_t ldx, int32_t Cin,
+__global__ void __launch_bounds__(kHT, 2) halo_fwd_kernel(FvgbGrid g, const T *__restrict__ x, int64_t ldx, int32_t Cin,
                                                        const T *__restrict__ w, int32_t Cout, int32_t mirror,
                                                        T *__restrict__ y, int64_t ldy) {
     using A = typename HNum<T>::A;
     constexpr int CC = HNum<T>::CC;
-    constexpr int RS = CC + 1;   // padded row stride of the staged halo (bank spread)
-    constexpr int kItems = 8;    // per thread: 512 voxels x 4 groups / 256 threads
+    constexpr int RS = CC + 1;  // padded row stride of the staged halo (bank spread)
     extern __shared__ __align__(16) uint8_t hsm[];
-    A *hbuf = reinterpret_cast<A *>(hsm);
-    A *wsm = hbuf + kHalo * RS;  // [27][CC][16]
-    int32_t *hslot = reinterpret_cast<int32_t *>(wsm + 27 * CC * kCoTile);
+    A *wsm = reinterpret_cast<A *>(hsm);  // [27][CC][16], 16-byte aligned rows
+    A *hbuf = wsm + 27 * CC * kCoTile;    // [active halo rows + 1 zero row][RS]
+    int32_t *hslot = reinterpret_cast<int32_t *>(hbuf + (kHalo + 1) * RS);
     int32_t *hrow = hslot + kHalo;
     int32_t *act_bit = hrow + kHalo;
     int32_t *act_row = act_bit + 512;
     int32_t *nbr = act_row + 512;
     int32_t *wcnt = nbr + 32;
     const int tid = threadIdx.x;
+    const int vg = tid >> 1, ch = (tid & 1) * 8;
     for (int64_t lf = blockIdx.x; lf < g.num_leaves; lf += gridDim.x) {
         __syncthreads();
         const int2 na = halo_setup(g, lf, hslot, hrow, act_bit, act_row, nbr, wcnt);
         const int n_act = na.x, n_halo = na.y;
-        const int n_items = 4 * n_act;
+        const bool busy = 4 * vg < n_act;
+        int hb[4];  // halo position of each of the thread's voxels (offset k adds off_k)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int a = 4 * vg + v;
+            const int bit = a < n_act ? act_bit[a] : 0;
+            hb[v] = ((bit >> 6) * 10 + ((bit >> 3) & 7)) * 10 + (bit & 7);
+        }
         for (int co0 = 0; co0 < Cout; co0 += kCoTile) {
-            A acc[kItems][4];
+            A acc[4][8];
 #pragma unroll
-            for (int it = 0; it < kItems; ++it)
+            for (int v = 0; v < 4; ++v)
 #pragma unroll
-                for (int e = 0; e < 4; ++e) acc[it][e] = (A)0;
+                for (int e = 0; e < 8; ++e) acc[v][e] = (A)0;
             for (int c0 = 0; c0 < Cin; c0 += CC) {
                 __syncthreads();
-                for (int e = tid; e < n_halo * CC; e += kHT) {
+                for (int e = tid; e < (n_halo + 1) * CC; e += kHT) {
                     const int sl = e / CC, ci = e % CC;
-                    hbuf[sl * RS + ci] = c0 + ci < Cin ? HNum<T>::to(x[(int64_t)hrow[sl] * ldx + c0 + ci]) : (A)0;
+                    hbuf[sl * RS + ci] = (sl < n_halo && c0 + ci < Cin)
+                                             ? HNum<T>::to(x[(int64_t)hrow[sl] * ldx + c0 + ci])
+                                             : (A)0;
                 }
                 for (int e = tid; e < 27 * CC * kCoTile; e += kHT) {
                     const int k = e / (CC * kCoTile), ci = (e / kCoTile) % CC, j = e % kCoTile;
@@ -180,36 +206,39 @@ __global__ void __launch_bounds__(kHT) halo_fwd_kernel(FvgbGrid g, const T *__re
                     wsm[e] = v;
                 }
                 __syncthreads();
-#pragma unroll
-                for (int it = 0; it < kItems; ++it) {
-                    const int item = tid + it * kHT;
-                    if (item >= n_items) break;
-                    const int a = item >> 2, q = item & 3;
-                    const int bit = act_bit[a];
-                    const int vx = bit >> 6, vy = (bit >> 3) & 7, vz = bit & 7;
+                if (busy) {
                     for (int k = 0; k < 27; ++k) {
-                        const int hp = ((vx + k / 9) * 10 + (vy + (k / 3) % 3)) * 10 + (vz + k % 3);
-                        const int sl = hslot[hp];
-                        if (sl < 0) continue;
-                        const A *hr = hbuf + sl * RS;
-                        const A *wr = wsm + k * CC * kCoTile + 4 * q;
+                        const int off = (k / 9) * 100 + ((k / 3) % 3) * 10 + (k % 3);
+                        int sl[4];
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) {
+                            const int q = hslot[hb[v] + off];
+                            sl[v] = (q < 0 ? n_halo : q) * RS;
+                        }
+                        const A *wk = wsm + k * CC * kCoTile + ch;
 #pragma unroll
                         for (int ci = 0; ci < CC; ++ci) {
-                            const A v = hr[ci];
+                            A wv[8];
+                            load8<A>(wk + ci * kCoTile, wv);
 #pragma unroll
-                            for (int e = 0; e < 4; ++e) acc[it][e] += v * wr[ci * kCoTile + e];
+                            for (int v = 0; v < 4; ++v) {
+                                const A h = hbuf[sl[v] + ci];
+#pragma unroll
+                                for (int e = 0; e < 8; ++e) acc[v][e] += h * wv[e];
+                            }
                         }
                     }
                 }
             }
 #pragma unroll
-            for (int it = 0; it < kItems; ++it) {
-                const int item = tid + it * kHT;
-                if (item >= n_items) break;
-                const int a = item >> 2, co = co0 + 4 * (item & 3);
+            for (int v = 0; v < 4; ++v) {
+                const int a = 4 * vg + v;
+                if (a >= n_act) continue;
 #pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    if (co + e < Cout) y[(int64_t)act_row[a] * ldy + co + e] = HNum<T>::from(acc[it][e]);
+                for (int e = 0; e < 8; ++e) {
+                    const int co = co0 + ch + e;
+                    if (co < Cout) y[(int64_t)act_row[a] * ldy + co] = HNum<T>::from(acc[v][e]);
+                }
             }
         }
     }

@@ -395,10 +395,96 @@ __global__ void masks_kernel(const int32_t *__restrict__ kmap, int64_t n_out, in
     if (threadIdx.x == 0 && tile_mask) tile_mask[blockIdx.x] = wm[0] | wm[1] | wm[2] | wm[3];
 }
 
+// Row order of the contraction tiles: rows sorted by their occupancy mask (descending), so the
+// 128 rows of a tile tend to share their present offsets and the per-tile mask skips more.
+__global__ void iota_kernel(int32_t *__restrict__ v, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (int32_t)i;
+}
+
+// tile t of the sorted order: OR of its rows' masks; padding rows of the last tile get -1
+__global__ void order_tiles_kernel(const uint32_t *__restrict__ sorted_mask, int64_t n_out, int32_t *__restrict__ rows,
+                                   uint32_t *__restrict__ tile_mask) {
+    __shared__ uint32_t wm[4];
+    const int64_t r = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    uint32_t m = r < n_out ? sorted_mask[r] : 0u;
+    if (r >= n_out) rows[r] = -1;
+    for (int o = 16; o > 0; o >>= 1) m |= __shfl_xor_sync(0xffffffffu, m, o);
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) tile_mask[blockIdx.x] = wm[0] | wm[1] | wm[2] | wm[3];
+}
+
+// map rows in the given order: out[128t + r] = kmap[rows[128t + r]] (-1 rows for padding)
+__global__ void permute_rows_kernel(const int32_t *__restrict__ kmap, int64_t ld, int32_t K,
+                                    const int32_t *__restrict__ rows, int64_t n_pad, int32_t *__restrict__ out) {
+    const int64_t total = n_pad * K;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / K;
+        const int k = (int)(e - r * K);
+        const int32_t src = rows[r];
+        out[e] = src >= 0 ? kmap[(int64_t)src * ld + k] : -1;
+    }
+}
+
 }  // namespace
 }  // namespace fvgb
 
 using namespace fvgb;
+
+extern "C" int fvgb_kmap_row_order_workspace(int64_t n_out, int32_t K, size_t *bytes) {
+    if (!bytes || n_out < 0 || n_out > INT32_MAX || K < 1 || K > 32) return FVGB_EINVAL;
+    size_t cub_bytes = 0;
+    if (cub::DeviceRadixSort::SortPairsDescending(nullptr, cub_bytes, (const uint32_t *)nullptr, (uint32_t *)nullptr,
+                                                  (const int32_t *)nullptr, (int32_t *)nullptr, (int)n_out, 0, K) !=
+        cudaSuccess)
+        return FVGB_ECUDA;
+    const size_t n = (size_t)n_out;
+    *bytes = n * 4 /* row masks */ + n * 4 /* sorted masks */ + n * 4 /* iota */ + cub_bytes + 4 * 256;
+    return FVGB_OK;
+}
+
+extern "C" int fvgb_kmap_row_order(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, int32_t *rows,
+                                   uint32_t *tile_mask, int32_t *sorted_map, void *workspace, size_t workspace_bytes,
+                                   fvgb_stream_t stream) {
+    size_t need = 0;
+    int st = fvgb_kmap_row_order_workspace(n_out, K, &need);
+    if (st) return st;
+    if (ld < K || !rows || !tile_mask) return FVGB_EINVAL;
+    if (n_out == 0) return FVGB_OK;
+    if (!kmap) return FVGB_EINVAL;
+    if (!workspace || workspace_bytes < need) return FVGB_ENOSPACE;
+    cudaStream_t s = as_stream(stream);
+    auto carve = [](uint8_t *&p, size_t bytes) {
+        uint8_t *q = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return q;
+    };
+    uint8_t *p = reinterpret_cast<uint8_t *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    const size_t n = (size_t)n_out;
+    uint32_t *mask = (uint32_t *)carve(p, n * 4);
+    uint32_t *smask = (uint32_t *)carve(p, n * 4);
+    int32_t *iota = (int32_t *)carve(p, n * 4);
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairsDescending(nullptr, cub_bytes, mask, smask, iota, rows, (int)n_out, 0, K, s);
+    if ((size_t)(p - (uint8_t *)workspace) + cub_bytes > workspace_bytes) return FVGB_ENOSPACE;
+    const unsigned tiles = (unsigned)ceil_div(n_out, 128);
+    masks_kernel<<<tiles, 128, 0, s>>>(kmap, n_out, K, ld, mask, nullptr);
+    iota_kernel<<<(unsigned)ceil_div(n_out, 256), 256, 0, s>>>(iota, n_out);
+    if (cub::DeviceRadixSort::SortPairsDescending(p, cub_bytes, mask, smask, iota, rows, (int)n_out, 0, K, s) !=
+        cudaSuccess)
+        return launch_status();
+    order_tiles_kernel<<<tiles, 128, 0, s>>>(smask, n_out, rows, tile_mask);
+    int launched = 3;
+    if (sorted_map) {
+        const int64_t n_pad = (int64_t)tiles * 128;
+        const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n_pad * K, 256), (int64_t)device_sm_count() * 16);
+        permute_rows_kernel<<<blocks, 256, 0, s>>>(kmap, ld, K, rows, n_pad, sorted_map);
+        ++launched;
+    }
+    count_launches(launched);
+    return launch_status();
+}
 
 extern "C" int fvgb_kmap_build(const FvgbGrid *src, const FvgbGrid *tgt, const int32_t ksize[3],
                                const int32_t stride[3], int32_t *kmap, int64_t ld, int32_t *nbsizes,

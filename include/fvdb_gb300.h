@@ -223,6 +223,21 @@ int fvgb_nbmap_build(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, 
 int fvgb_kmap_masks(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, uint32_t *row_mask,
                     uint32_t *tile_mask, fvgb_stream_t stream);
 
+/*
+ * Row order for the contractions (K <= 32): the rows of kmap sorted by occupancy mask, descending
+ * (a stable radix sort), so that the 128 rows of a contraction tile tend to share their present
+ * offsets and the per-tile mask skips more of the reduction.  rows [ceil(n_out/128)*128] receives
+ * the order (padding -1), tile_mask [ceil(n_out/128)] the OR of each ordered tile's row masks,
+ * and sorted_map (optional, [ceil(n_out/128)*128, K]) the map's rows in that order (-1 rows for
+ * padding), which the *_rows contractions read tile by tile.  The sorted-mask / reorder_loc /
+ * reordered out_in_map of the reference's sorted implicit GEMM (SparseConvPackInfo.cpp:110-147,
+ * IGEMMBitOperations.cu:14-90), computed on the device.
+ */
+int fvgb_kmap_row_order_workspace(int64_t n_out, int32_t K, size_t *bytes);
+int fvgb_kmap_row_order(const int32_t *kmap, int64_t n_out, int32_t K, int64_t ld, int32_t *rows,
+                        uint32_t *tile_mask, int32_t *sorted_map, void *workspace, size_t workspace_bytes,
+                        fvgb_stream_t stream);
+
 /* ---------------------------------------------------------------- contractions --- */
 
 /*
@@ -241,6 +256,13 @@ int fvgb_conv_fwd_simt(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, 
                        const int32_t *map, int64_t n_out, int32_t K, int64_t ldm, const void *w,
                        int64_t wsk, int64_t wsci, int64_t wsco, void *y, int32_t c_out,
                        int64_t ldy, int32_t accumulate, fvgb_stream_t stream);
+/* fvgb_conv_fwd_simt over 128-row tiles of a given row order (map and rows as for
+ * fvgb_conv_fwd_tc_rows, padded to a multiple of 128 rows): each output row is computed exactly
+ * as in index order; offsets absent from a whole tile are skipped. */
+int fvgb_conv_fwd_simt_rows(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx, const int32_t *map,
+                            int64_t n_out, int32_t K, int64_t ldm, const int32_t *rows, const void *w, int64_t wsk,
+                            int64_t wsci, int64_t wsco, void *y, int32_t c_out, int64_t ldy, int32_t accumulate,
+                            fvgb_stream_t stream);
 
 /*
  * Weight gradient on CUDA cores:  dW[k, ci, co] = sum_m x[map[m,k], ci] * dy[m, co].
@@ -335,6 +357,18 @@ int fvgb_conv_fwd_tc_epilogue(int32_t dtype, const void *x, int64_t n_x, int32_t
                               const int32_t *map, int64_t n_out, int32_t K, const uint32_t *tile_mask,
                               const void *packed_w, int32_t c_out, void *y, int64_t ldy, const float *out_scale,
                               const float *bias, int32_t relu, int32_t *err_dev, fvgb_stream_t stream);
+
+/*
+ * fvgb_conv_fwd_tc_epilogue over tiles of a given row order: `map` holds the rows in that order
+ * (fvgb_kmap_row_order's sorted_map), row 128t + r of it computes output row rows[128t + r]
+ * (-1 = none), and tile_mask is that order's.  Each output row is computed exactly as in the
+ * index order (same units, same order), so the result is the same; rows are stored one by one.  Replaces the sorted implicit-GEMM forward
+ * (SparseConvolutionImplicitGEMMSorted.cu:115-2979, its reorder_loc gather / scatter).
+ */
+int fvgb_conv_fwd_tc_rows(int32_t dtype, const void *x, int64_t n_x, int32_t c_in, int64_t ldx, const int32_t *map,
+                          int64_t n_out, int32_t K, const int32_t *rows, const uint32_t *tile_mask,
+                          const void *packed_w, int32_t c_out, void *y, int64_t ldy, const float *out_scale,
+                          const float *bias, int32_t relu, int32_t *err_dev, fvgb_stream_t stream);
 
 /*
  * Tile plan of a kernel map for the planned tensor-core convolution: for every 128-row tile of

@@ -124,8 +124,9 @@ def test_planned_forward_multi_phase_bf16(cuda_device, cin, cout):
     g = torch.Generator().manual_seed(cin + cout)
     x = torch.randn(src.total_voxels, cin, generator=g).bfloat16()
     w = (torch.randn(cout, cin, 3, 3, 3, generator=g) * math.sqrt(2.0 / (27 * cin))).bfloat16()
-    # the first contraction on the map runs unplanned, the second over the (then built) plan:
-    # both issue the same MMAs in the same order, so they agree bit for bit
+    # the first contraction on the map runs in index order, the second over the map's (then
+    # built) row order: both issue the same MMAs per row in the same order, so they agree bit for
+    # bit; the planned kernel over this map is checked through the C ABI below
     y0 = pack.sparse_conv_3d(x.to(cuda_device), w.to(cuda_device)).jdata
     y = pack.sparse_conv_3d(x.to(cuda_device), w.to(cuda_device)).jdata
     torch.cuda.synchronize()
@@ -140,7 +141,8 @@ def test_planned_forward_multi_phase_bf16(cuda_device, cin, cout):
 
 
 def test_planned_dgrad_multi_phase_bf16(cuda_device):
-    """Data gradient over the transposed map's plan, lattice case: rel-L2 <= 1e-2 vs FP64."""
+    """Data gradient over the transposed map, first in index order then over its row order (bitwise
+    equal), lattice case: rel-L2 <= 1e-2 vs FP64."""
     src, tgt, pack = _lattice_case(cuda_device)
     s = src.ijk.jdata.cpu().numpy()
     t = tgt.ijk.jdata.cpu().numpy()
@@ -150,7 +152,7 @@ def test_planned_dgrad_multi_phase_bf16(cuda_device):
     w = (torch.randn(32, 32, 3, 3, 3, generator=g) * 0.05).bfloat16()
     dy = torch.randn(tgt.total_voxels, 32, generator=g).bfloat16()
     grads = []
-    for _ in range(2):  # the second backward runs over the transposed map's plan
+    for _ in range(2):  # the second backward runs over the transposed map's row order
         xt = x.to(cuda_device).requires_grad_(True)
         y = pack.sparse_conv_3d(xt, w.to(cuda_device)).jdata
         y.backward(dy.to(cuda_device))
@@ -161,7 +163,8 @@ def test_planned_dgrad_multi_phase_bf16(cuda_device):
 
 
 def test_planned_fp8_multi_phase(cuda_device):
-    """FP8-E4M3 over a multi-phase plan: within the E4M3 bound of the FP64 oracle (rel-L2 <= 8e-2)."""
+    """FP8-E4M3 on the lattice map, index order then row order (bitwise equal): within the E4M3
+    bound of the FP64 oracle (rel-L2 <= 8e-2)."""
     import fvdb
 
     src, tgt, pack = _lattice_case(cuda_device)
@@ -173,7 +176,7 @@ def test_planned_fp8_multi_phase(cuda_device):
     w = (torch.randn(64, 64, 3, 3, 3, generator=g) * math.sqrt(2.0 / (27 * 64))).bfloat16()
     C = fvdb._lib.load()
     y0, _, _ = C.conv_forward_fp8(x.to(cuda_device), w.to(cuda_device), pack._impl, False)
-    y, _, _ = C.conv_forward_fp8(x.to(cuda_device), w.to(cuda_device), pack._impl, False)  # over the plan
+    y, _, _ = C.conv_forward_fp8(x.to(cuda_device), w.to(cuda_device), pack._impl, False)  # over the row order
     torch.cuda.synchronize()
     assert torch.equal(y0, y)
     C.check_device_errors(cuda_device)
@@ -181,7 +184,8 @@ def test_planned_fp8_multi_phase(cuda_device):
     assert rel_l2(y.double().cpu().numpy(), ref) <= 8e-2
 
 
-@pytest.mark.parametrize("case,cin,cout", [("sparse", 32, 64), ("lattice", 64, 32), ("sparse", 96, 128)])
+@pytest.mark.parametrize("case,cin,cout", [("sparse", 32, 64), ("lattice", 64, 32), ("sparse", 96, 128),
+                                           ("lattice", 16, 32), ("lattice", 32, 64), ("lattice", 128, 64)])
 def test_planned_through_c_abi_equals_unplanned(cuda_device, case, cin, cout):
     """fvgb_tc_plan_build + fvgb_conv_fwd_tc_planned with raw pointers: bitwise equal to
     fvgb_conv_fwd_tc_bias on the same map, weights and bias, and within 5e-3 rel-L2 of FP64."""
