@@ -634,6 +634,44 @@ def leg_halo(fvdb, grid, x, model, args) -> dict:
     return out
 
 
+def probe_row_gather(args) -> None:
+    """Random 128-byte row gathers into the tensor-core A-operand layout (fvgb_row_gather_probe): a
+    2M-row x 128-byte feature table (256 MB, larger than L2), 2^20 random row indices, one CTA per
+    SM gathering 512 stages of 128 rows; best of 3 launches per method, timed with CUDA events.
+    Prints one JSON line."""
+    import ctypes
+
+    from fvdb import _lib
+
+    lib = _lib.cdll()
+    n = 2 * 1024 * 1024
+    x = torch.randn(n, 64, device="cuda").bfloat16()
+    rows = torch.randint(0, n, (1 << 20,), generator=torch.Generator().manual_seed(0), dtype=torch.int32).cuda()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    nbytes = ctypes.c_int64(0)
+    out = {}
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for mode, name in ((3, "cp_async_8_warps"), (1, "gather4_lane0_of_8_warps"), (2, "gather4_32_lanes_of_1_warp"),
+                       (0, "gather4_1_thread")):
+        best = None
+        for _ in range(3):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            rc = lib.fvgb_row_gather_probe(mode, ctypes.c_void_p(x.data_ptr()), ctypes.c_int64(n),
+                                           ctypes.c_void_p(rows.data_ptr()), rows.numel(), 512,
+                                           ctypes.c_void_p(err.data_ptr()), ctypes.byref(nbytes), stream)
+            b.record()
+            torch.cuda.synchronize()
+            assert rc == 0 and int(err.item()) == 0, (rc, int(err.item()))
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = {"ms": best, "GB_per_s": nbytes.value / (best * 1e-3) / 1e9,
+                     "ns_per_16KB_stage_per_SM": best * 1e6 / (512.0)}
+    print(json.dumps({"probe": "random 128-byte row gather into a 128B-swizzled shared-memory stage",
+                      "sms": sms, "stages_per_sm": 512, "results": out}))
+
+
 def box_surface_ijk(n_boxes: int, resolution: int, seed: int, device) -> torch.Tensor:
     """Faces of n random axis-aligned boxes (sides U[0.1,0.5], min corner U[0,1-side]) at resolution^3."""
     g = torch.Generator().manual_seed(seed)
@@ -882,7 +920,12 @@ def main():
                     help="voxels of the FP8 leg's grid (4M is the stated size; smaller only for profiling captures)")
     ap.add_argument("--points", type=int, default=2_000_000,
                     help="points per grid (the headline workload uses 2M; smaller only for profiling captures)")
+    ap.add_argument("--probe-gather", action="store_true",
+                    help="only run the row-gather probe (cp.async vs TMA gather4) and print its JSON line")
     args = ap.parse_args()
+    if args.probe_gather:
+        probe_row_gather(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -448,35 +448,3 @@ extern "C" int fvgb_conv_wgrad_simt_noalloc(int32_t dtype, const void *x, int64_
     count_launches(n_out > 0 ? 2 : 1);
     return launch_status();
 }
-
-// ---------------------------------------------------------------------------------------------
-// FP32 FMA rate probe: every thread runs 8 independent fma chains of `iters` steps (enough
-// independent work to keep the FMA pipes full), 2 * 8 * iters FLOPs per thread.  The caller
-// times the launch; the chains' sum is written so that nothing is optimised away.
-namespace fvgb {
-namespace {
-__global__ void __launch_bounds__(256) ffma_probe_kernel(float *out, int64_t iters, float b, float c) {
-    float v[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = (float)(threadIdx.x + i);
-    for (int64_t it = 0; it < iters; ++it) {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) v[i] = fmaf(v[i], b, c);
-    }
-    float s = 0.f;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) s += v[i];
-    if (s == 12345.678f) out[0] = s;  // practically never true: keeps the chains live
-    if (threadIdx.x == 0 && blockIdx.x == 0) out[1] = s;
-}
-}  // namespace
-}  // namespace fvgb
-
-extern "C" int fvgb_ffma_probe(float *out, int64_t iters, int32_t blocks_per_sm, double *flops, fvgb_stream_t stream) {
-    if (!out || iters < 1 || blocks_per_sm < 1 || blocks_per_sm > 64 || !flops) return FVGB_EINVAL;
-    const int64_t blocks = (int64_t)device_sm_count() * blocks_per_sm;
-    ffma_probe_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(out, iters, 0.999999f, 1e-7f);
-    *flops = 2.0 * 8.0 * (double)iters * 256.0 * (double)blocks;
-    count_launches(1);
-    return launch_status();
-}

@@ -29,7 +29,7 @@ LIB_NAME = "libfvdb_gb300.so"
 EXT_NAME = "fvdb_gb300_C"
 
 CUDA_UNITS = ["abi.cu", "grid.cu", "kmap.cu", "conv_simt.cu", "conv_fwd_tc.cu", "conv_fwd_plan.cu", "conv_tc.cu", "pool.cu",
-              "halo.cu"]
+              "halo.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

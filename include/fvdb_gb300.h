@@ -485,6 +485,15 @@ int fvgb_subdivide_candidates(const FvgbGrid *coarse, const int32_t factor[3], c
  * *flops (host) = FLOPs of the launch, which the caller times on `stream`.  out: device float[2].
  * No counterpart in the reference. */
 int fvgb_ffma_probe(float *out, int64_t iters, int32_t blocks_per_sm, double *flops, fvgb_stream_t stream);
+/* Row-gather probe (for the design notes: how fast random 128-byte feature rows reach a
+ * 128B-swizzled shared-memory stage): one CTA of 256 threads per SM gathers `iters` stages of 128
+ * rows (row indices rows[0..nlist), cycled) of x [n_rows, 128 B] into a 4-deep ring; mode 0/1/2:
+ * TMA tile::gather4 issued by 1 thread / lane 0 of 8 warps / 32 lanes of one warp, mode 3:
+ * cp.async by 8 warps.  *bytes (host) = bytes moved by the launch, which the caller times on
+ * `stream`; *err_dev (zeroed device int32) becomes FVGB_ETIMEOUT if a bounded wait gave up.  x
+ * 128-byte aligned.  No counterpart in the reference. */
+int fvgb_row_gather_probe(int32_t mode, const void *x, int64_t n_rows, const int32_t *rows, int32_t nlist,
+                          int32_t iters, int32_t *err_dev, int64_t *bytes, fvgb_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
  * Leaf-halo convolution: stride-1 3x3x3 convolution of a grid onto itself with no kernel map.
