@@ -636,15 +636,15 @@ def leg_halo(fvdb, grid, x, model, args) -> dict:
 
 def probe_row_gather(args) -> None:
     """Random 128-byte row gathers into the tensor-core A-operand layout (fvgb_row_gather_probe): a
-    2M-row x 128-byte feature table (256 MB, larger than L2), 2^20 random row indices, one CTA per
-    SM gathering 512 stages of 128 rows; best of 3 launches per method, timed with CUDA events.
-    Prints one JSON line."""
+    feature table of --probe-gather-rows rows x 128 bytes (default 2M = 256 MB, larger than L2),
+    2^20 random row indices, one CTA per SM gathering 512 stages of 128 rows; best of 3 launches
+    per method, timed with CUDA events.  Prints one JSON line."""
     import ctypes
 
     from fvdb import _lib
 
     lib = _lib.cdll()
-    n = 2 * 1024 * 1024
+    n = args.probe_gather_rows
     x = torch.randn(n, 64, device="cuda").bfloat16()
     rows = torch.randint(0, n, (1 << 20,), generator=torch.Generator().manual_seed(0), dtype=torch.int32).cuda()
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -653,7 +653,7 @@ def probe_row_gather(args) -> None:
     out = {}
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     for mode, name in ((3, "cp_async_8_warps"), (1, "gather4_lane0_of_8_warps"), (2, "gather4_32_lanes_of_1_warp"),
-                       (0, "gather4_1_thread")):
+                       (0, "gather4_1_thread"), (4, "half_gather4_half_cp_async")):
         best = None
         for _ in range(3):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -669,7 +669,7 @@ def probe_row_gather(args) -> None:
         out[name] = {"ms": best, "GB_per_s": nbytes.value / (best * 1e-3) / 1e9,
                      "ns_per_16KB_stage_per_SM": best * 1e6 / (512.0)}
     print(json.dumps({"probe": "random 128-byte row gather into a 128B-swizzled shared-memory stage",
-                      "sms": sms, "stages_per_sm": 512, "results": out}))
+                      "table_rows": n, "table_mb": n * 128 / 1e6, "sms": sms, "stages_per_sm": 512, "results": out}))
 
 
 def box_surface_ijk(n_boxes: int, resolution: int, seed: int, device) -> torch.Tensor:
@@ -922,6 +922,8 @@ def main():
                     help="points per grid (the headline workload uses 2M; smaller only for profiling captures)")
     ap.add_argument("--probe-gather", action="store_true",
                     help="only run the row-gather probe (cp.async vs TMA gather4) and print its JSON line")
+    ap.add_argument("--probe-gather-rows", type=int, default=2 * 1024 * 1024,
+                    help="rows of 128 bytes in the probe's table (2M = 256 MB, beyond L2; 256k = 32 MB fits L2)")
     args = ap.parse_args()
     if args.probe_gather:
         probe_row_gather(args)

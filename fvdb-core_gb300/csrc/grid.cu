@@ -554,3 +554,207 @@ extern "C" int fvgb_ijk_to_index(const FvgbGrid *grid, const int32_t *ijk, const
     count_launches(1);
     return launch_status();
 }
+
+// ---------------------------------------------------------------------------------------------
+// Coarse grid of floor(ijk / f) built leaf by leaf, for power-of-two factors f <= 8 per axis: a
+// fine leaf (8^3 voxels) falls inside one coarse leaf, so the fine leaves are grouped by coarse
+// leaf (a radix sort of one key per fine leaf, not per voxel), each coarse leaf's occupancy mask
+// is the OR of its fine leaves' voxels mapped down, and the coarse voxels are written leaf by
+// leaf in bit order.  Coarse leaves sorted by (grid, order key) and voxels by bit within a leaf
+// is the NanoVDB index order: the result is identical to sorting floor(ijk / f) voxel by voxel.
+namespace fvgb {
+namespace {
+
+constexpr int kCoarseMaxGrids = 1024;  // the grid index takes the key's top 10 bits
+
+struct CoarseWs {
+    uint64_t *keys_a, *keys_b, *cmask;
+    int32_t *vals_a, *vals_b, *cid, *count, *base;
+    int4 *corig;
+    void *cub_tmp;
+    size_t cub_bytes;
+};
+
+size_t coarse_ws_layout(int64_t nl, CoarseWs *w, char *base) {
+    size_t cub_bytes = 0, c = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, c, (uint64_t *)nullptr, (uint64_t *)nullptr, (int32_t *)nullptr,
+                                    (int32_t *)nullptr, (int)nl, 0, 64);
+    cub_bytes = c;
+    cub::DeviceScan::InclusiveSum(nullptr, c, (int32_t *)nullptr, (int32_t *)nullptr, (int)nl);
+    if (c > cub_bytes) cub_bytes = c;
+    cub::DeviceScan::ExclusiveSum(nullptr, c, (int32_t *)nullptr, (int32_t *)nullptr, (int)nl + 1);
+    if (c > cub_bytes) cub_bytes = c;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = base ? base + off : nullptr;
+        off += (bytes + 255) & ~(size_t)255;
+        return p;
+    };
+    const size_t n = (size_t)nl;
+    char *ka = take(n * 8), *kb = take(n * 8), *cm = take(n * 64), *va = take(n * 4), *vb = take(n * 4),
+         *ci = take((n + 1) * 4), *co = take((n + 1) * 4), *ba = take((n + 1) * 4), *og = take(n * 16),
+         *tmp = take(cub_bytes);
+    if (w) {
+        w->keys_a = (uint64_t *)ka, w->keys_b = (uint64_t *)kb, w->cmask = (uint64_t *)cm;
+        w->vals_a = (int32_t *)va, w->vals_b = (int32_t *)vb, w->cid = (int32_t *)ci, w->count = (int32_t *)co;
+        w->base = (int32_t *)ba, w->corig = (int4 *)og, w->cub_tmp = tmp, w->cub_bytes = cub_bytes;
+    }
+    return off;
+}
+
+// key of fine leaf l: (grid << 54) | (order key of its coarse leaf's origin >> 9)
+__global__ void coarse_keys_kernel(const FvgbLeaf *__restrict__ leaves, int64_t nl, int3 sh,
+                                   uint64_t *__restrict__ keys, int32_t *__restrict__ vals) {
+    const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nl) return;
+    const FvgbLeaf &lf = leaves[l];
+    const int32_t cx = (lf.origin[0] >> (sh.x + 3)) << 3, cy = (lf.origin[1] >> (sh.y + 3)) << 3,
+                  cz = (lf.origin[2] >> (sh.z + 3)) << 3;
+    keys[l] = ((uint64_t)lf.batch << 54) | (order_key(cx, cy, cz) >> 9);
+    vals[l] = (int32_t)l;
+}
+
+__global__ void coarse_flags_kernel(const uint64_t *__restrict__ keys, int64_t nl, int32_t *__restrict__ flags) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nl) return;
+    flags[p] = (p == 0 || keys[p] != keys[p - 1]) ? 1 : 0;
+}
+
+// warp per sorted fine leaf: OR its voxels, mapped down, into its coarse leaf's mask
+__global__ void coarse_mask_kernel(const FvgbLeaf *__restrict__ leaves, int64_t nl, int3 sh,
+                                   const int32_t *__restrict__ vals, const int32_t *__restrict__ cid,
+                                   uint64_t *__restrict__ cmask, int4 *__restrict__ corig) {
+    __shared__ unsigned long long wm[8][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t p = (int64_t)blockIdx.x * 8 + warp;
+    if (p >= nl) return;  // whole warps leave together
+    const FvgbLeaf &lf = leaves[vals[p]];
+    const int32_t c = cid[p] - 1;
+    if (lane < 8) wm[warp][lane] = 0ull;
+    __syncwarp();
+    const uint64_t word = lf.mask[lane >> 2];
+    const int sub = (lane & 3) * 16;
+    for (int i = 0; i < 16; ++i) {
+        if (!((word >> (sub + i)) & 1ull)) continue;
+        const int b = (lane >> 2) * 64 + sub + i;
+        const int32_t gx = lf.origin[0] + (b >> 6), gy = lf.origin[1] + ((b >> 3) & 7), gz = lf.origin[2] + (b & 7);
+        const uint32_t cb = leaf_bit(gx >> sh.x, gy >> sh.y, gz >> sh.z);
+        atomicOr(&wm[warp][cb >> 6], 1ull << (cb & 63));
+    }
+    __syncwarp();
+    if (lane < 8) {
+        const unsigned long long m = wm[warp][lane];
+        if (m) atomicOr(reinterpret_cast<unsigned long long *>(cmask) + (int64_t)c * 8 + lane, m);
+    }
+    if (lane == 0)  // every fine leaf of coarse leaf c writes the same origin
+        corig[c] = make_int4((lf.origin[0] >> (sh.x + 3)) << 3, (lf.origin[1] >> (sh.y + 3)) << 3,
+                             (lf.origin[2] >> (sh.z + 3)) << 3, lf.batch);
+}
+
+// voxels per coarse leaf (zero past the coarse-leaf count, for the exclusive scan over nl + 1)
+__global__ void coarse_count_kernel(const uint64_t *__restrict__ cmask, const int32_t *__restrict__ cid, int64_t nl,
+                                    int32_t *__restrict__ count) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > nl) return;
+    const int64_t lc = cid[nl - 1];
+    int32_t n = 0;
+    if (c < lc)
+#pragma unroll
+        for (int w = 0; w < 8; ++w) n += __popcll(cmask[c * 8 + w]);
+    count[c] = n;
+}
+
+// warp per coarse leaf: its voxels in bit order, and their leaf ids (1-based)
+__global__ void coarse_emit_kernel(const uint64_t *__restrict__ cmask, const int4 *__restrict__ corig,
+                                   const int32_t *__restrict__ cid, const int32_t *__restrict__ base, int64_t nl,
+                                   int32_t *__restrict__ out_ijk, int32_t *__restrict__ leaf_ids) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c = (int64_t)blockIdx.x * 8 + warp;
+    if (c >= nl || c >= cid[nl - 1]) return;
+    const int w = lane >> 2, sub = (lane & 3) * 16;
+    int32_t rank = base[c];
+    for (int v = 0; v < w; ++v) rank += __popcll(cmask[c * 8 + v]);
+    const uint64_t word = cmask[c * 8 + w];
+    rank += __popcll(sub ? (word & ((1ull << sub) - 1ull)) : 0ull);
+    const int4 o = corig[c];
+    for (int i = 0; i < 16; ++i) {
+        if (!((word >> (sub + i)) & 1ull)) continue;
+        const int b = w * 64 + sub + i;
+        out_ijk[3 * (int64_t)rank] = o.x + (b >> 6);
+        out_ijk[3 * (int64_t)rank + 1] = o.y + ((b >> 3) & 7);
+        out_ijk[3 * (int64_t)rank + 2] = o.z + (b & 7);
+        leaf_ids[rank] = (int32_t)c + 1;
+        ++rank;
+    }
+}
+
+// meta[b] = first voxel of grid b (b <= B), meta[B+1] = coarse leaves, meta[B+2] = voxels
+__global__ void coarse_offsets_kernel(const int4 *__restrict__ corig, const int32_t *__restrict__ cid,
+                                      const int32_t *__restrict__ base, int64_t nl, int32_t B,
+                                      int64_t *__restrict__ meta) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > B) return;
+    const int64_t lc = cid[nl - 1];
+    int64_t lo = 0, hi = lc;  // first coarse leaf with grid >= b
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (corig[mid].w < b) lo = mid + 1; else hi = mid;
+    }
+    meta[b] = base[lo];
+    if (b == 0) {
+        meta[B + 1] = lc;
+        meta[B + 2] = base[lc];
+    }
+}
+
+}  // namespace
+}  // namespace fvgb
+
+extern "C" int fvgb_coarse_grid_workspace(int64_t num_fine_leaves, size_t *bytes) {
+    if (!bytes || num_fine_leaves < 0 || num_fine_leaves >= INT32_MAX) return FVGB_EINVAL;
+    *bytes = fvgb::coarse_ws_layout(std::max<int64_t>(num_fine_leaves, 1), nullptr, nullptr) + 256;
+    return FVGB_OK;
+}
+
+extern "C" int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor[3], int32_t *out_ijk,
+                                      int64_t *meta, int32_t *leaf_ids, void *workspace, size_t workspace_bytes,
+                                      fvgb_stream_t stream) {
+    if (!fine || !factor || !meta) return FVGB_EINVAL;
+    if (fine->num_grids < 1 || fine->num_grids > kCoarseMaxGrids) return FVGB_EINVAL;
+    int sh[3];
+    for (int a = 0; a < 3; ++a) {
+        const int f = factor[a];
+        if (f != 1 && f != 2 && f != 4 && f != 8) return FVGB_EINVAL;
+        sh[a] = f == 1 ? 0 : (f == 2 ? 1 : (f == 4 ? 2 : 3));
+    }
+    const int64_t nl = fine->num_leaves;
+    if (nl == 0) return FVGB_EINVAL;  // callers handle empty grids themselves
+    if (!out_ijk || !leaf_ids || !fine->leaves) return FVGB_EINVAL;
+    size_t need = 0;
+    int st = fvgb_coarse_grid_workspace(nl, &need);
+    if (st) return st;
+    if (!workspace || workspace_bytes < need) return FVGB_ENOSPACE;
+    cudaStream_t s = as_stream(stream);
+    char *base = reinterpret_cast<char *>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    CoarseWs w;
+    coarse_ws_layout(nl, &w, base);
+    const int3 shv = make_int3(sh[0], sh[1], sh[2]);
+    if (cudaMemsetAsync(w.cmask, 0, (size_t)nl * 64, s) != cudaSuccess) return launch_status();
+    coarse_keys_kernel<<<blocks_for(nl), kThreads, 0, s>>>(fine->leaves, nl, shv, w.keys_a, w.vals_a);
+    size_t tb = w.cub_bytes;
+    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.vals_a, w.vals_b, (int)nl, 0, 64, s);
+    coarse_flags_kernel<<<blocks_for(nl), kThreads, 0, s>>>(w.keys_b, nl, w.count);
+    tb = w.cub_bytes;
+    cub::DeviceScan::InclusiveSum(w.cub_tmp, tb, w.count, w.cid, (int)nl, s);
+    coarse_mask_kernel<<<(unsigned)ceil_div(nl, 8), 256, 0, s>>>(fine->leaves, nl, shv, w.vals_b, w.cid, w.cmask,
+                                                                w.corig);
+    coarse_count_kernel<<<blocks_for(nl + 1), kThreads, 0, s>>>(w.cmask, w.cid, nl, w.count);
+    tb = w.cub_bytes;
+    cub::DeviceScan::ExclusiveSum(w.cub_tmp, tb, w.count, w.base, (int)nl + 1, s);
+    coarse_emit_kernel<<<(unsigned)ceil_div(nl, 8), 256, 0, s>>>(w.cmask, w.corig, w.cid, w.base, nl, out_ijk,
+                                                                leaf_ids);
+    coarse_offsets_kernel<<<(unsigned)ceil_div(fine->num_grids + 1, kThreads), kThreads, 0, s>>>(
+        w.corig, w.cid, w.base, nl, fine->num_grids, meta);
+    count_launches(7);
+    return launch_status();
+}

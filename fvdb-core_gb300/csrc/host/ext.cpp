@@ -257,6 +257,52 @@ GridPtr grid_from_points(const Tensor &points, const Tensor &joffsets, const Ten
     return build_grid(ijk, joff, vsb, orb);
 }
 
+// Coarse grid floor(ijk / f) of a grid, built leaf by leaf (fvgb_coarse_grid_build: one sort
+// key per fine leaf instead of one per voxel; the same voxels in the same order as sorting the
+// coarsened voxels).  f per axis in {1, 2, 4, 8}; lo/hi: bounds of the coarse voxels.
+GridPtr build_coarse_by_leaves(const GridPtr &g, const Vec3 &f, const int32_t lo[3], const int32_t hi[3]) {
+    auto dev = g->device();
+    const int64_t B = g->B;
+    auto c = std::make_shared<GridImpl>();
+    c->B = B;
+    c->voxel_sizes = g->voxel_sizes.clone();
+    c->origins = g->origins.clone();
+    auto i32 = torch::dtype(torch::kInt32).device(dev);
+    Tensor out_ijk = torch::empty({std::max<int64_t>(g->N, 1), 3}, i32);
+    Tensor leaf_ids = torch::empty({std::max<int64_t>(g->N, 1)}, i32);
+    Tensor meta = torch::zeros({B + 4}, torch::dtype(torch::kInt64).device(dev));
+    size_t wsb = 0;
+    check_status(fvgb_coarse_grid_workspace(g->L, &wsb), "coarse grid (workspace)");
+    Tensor ws = workspace(wsb, dev);
+    FvgbGrid fv = g->view();
+    auto s = cur_stream();
+    check_status(fvgb_coarse_grid_build(&fv, f.v, out_ijk.data_ptr<int32_t>(), meta.data_ptr<int64_t>(),
+                                        leaf_ids.data_ptr<int32_t>(), ws.data_ptr(), ws.numel(), s),
+                 "coarse grid");
+    int64_t *h = pinned_meta(dev.index(), (size_t)(B + 4));
+    cudaStream_t cs = reinterpret_cast<cudaStream_t>(s);
+    TORCH_CHECK(cudaMemcpyAsync(h, meta.data_ptr<int64_t>(), (B + 4) * sizeof(int64_t), cudaMemcpyDeviceToHost, cs) ==
+                        cudaSuccess &&
+                    cudaStreamSynchronize(cs) == cudaSuccess,
+                "coarse grid: reading the counts failed");
+    for (int a = 0; a < 3; ++a) {
+        c->box_lo[a] = lo[a];
+        c->box_hi[a] = hi[a];
+    }
+    c->joffsets_host = torch::from_blob(h, {B + 1}, torch::kInt64).clone();
+    c->joffsets = meta.narrow(0, 0, B + 1);
+    c->N = h[B + 2];
+    c->ijk = out_ijk.narrow(0, 0, c->N);
+    c->L = h[B + 1];
+    c->cap = next_pow2(2 * c->L);
+    c->leaves = torch::empty({std::max<int64_t>(c->L, 1) * (int64_t)sizeof(FvgbLeaf)},
+                             torch::dtype(torch::kUInt8).device(dev));
+    c->hash = torch::empty({c->cap}, i32);
+    FvgbGrid v = c->view();
+    check_status(fvgb_grid_index_build(&v, leaf_ids.data_ptr<int32_t>(), s), "coarse grid (index)");
+    return c;
+}
+
 // conv_grid: output voxel set of a (strided) convolution (BuildGridForConv.cu:181-255).
 GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, const std::vector<int64_t> &st_in) {
     c10::cuda::CUDAGuard guard(g->device());
@@ -271,6 +317,21 @@ GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, cons
     auto dev = g->device();
     const bool coarse = (st.v[0] == 1 && st.v[1] == 1 && st.v[2] == 1) ||
                         (st.v[0] == ks.v[0] && st.v[1] == ks.v[1] && st.v[2] == ks.v[2]);
+    auto fdiv = [](int64_t a, int64_t b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
+    // the coarse path with power-of-two strides <= 8: built leaf by leaf
+    bool pow2 = coarse && g->N > 0 && g->L > 0 && g->B <= 1024;
+    for (int a = 0; a < 3; ++a) {
+        const int v = st.v[a];
+        pow2 = pow2 && (v == 1 || v == 2 || v == 4 || v == 8);
+    }
+    if (pow2 && !(st.v[0] == 1 && st.v[1] == 1 && st.v[2] == 1)) {
+        int32_t lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = (int32_t)fdiv(g->box_lo[a], st.v[a]);
+            hi[a] = (int32_t)fdiv(g->box_hi[a], st.v[a]);
+        }
+        return build_coarse_by_leaves(g, st, lo, hi);
+    }
     const int64_t kc = coarse ? 1 : (int64_t)ks.v[0] * ks.v[1] * ks.v[2];
     const int64_t n = g->N * kc;
     auto i32 = torch::dtype(torch::kInt32).device(dev);
@@ -300,7 +361,6 @@ GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, cons
     // bounds of the candidates from the source grid's bounding box: floor(ijk/s) per axis on the
     // coarse path; (ijk + offset)/s over the footprint otherwise (k0 and s0 act on axis 2)
     if (g->N == 0) return build_grid(ijk, joff, g->voxel_sizes, g->origins);
-    auto fdiv = [](int64_t a, int64_t b) { return a >= 0 ? a / b : -((-a + b - 1) / b); };
     int32_t lo[3], hi[3];
     for (int a = 0; a < 3; ++a) {
         if (coarse) {

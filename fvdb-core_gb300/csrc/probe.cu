@@ -59,7 +59,8 @@ __device__ __forceinline__ void gather4_load(uint32_t dst, const void *tmap, int
 }
 
 // mode 0: one thread issues the 32 gather4 of a stage; 1: lane 0 of each of the 8 warps, 4 each;
-// 2: the 32 lanes of warp 0, 1 each; 3: cp.async by the 8 warps (lane -> 16-byte piece of 4 rows)
+// 2: the 32 lanes of warp 0, 1 each; 3: cp.async by the 8 warps (lane -> 16-byte piece of 4 rows);
+// 4: both at once, rows 0-63 by gather4 (16 lanes of warp 0), rows 64-127 by cp.async (warps 4-7)
 __global__ void __launch_bounds__(256, 1) row_gather_probe_kernel(const __grid_constant__ CUtensorMap tm,
                                                                   const uint8_t *__restrict__ x,
                                                                   const int32_t *__restrict__ rows, int32_t nlist,
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(256, 1) row_gather_probe_kernel(const __grid_c
     uint64_t *full = reinterpret_cast<uint64_t *>(base + kProbeStages * kProbeStage);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0)
-        for (int s = 0; s < kProbeStages; ++s) mbar_init(&full[s], mode == 3 ? 256 : 1);
+        for (int s = 0; s < kProbeStages; ++s) mbar_init(&full[s], mode == 3 ? 256 : (mode == 4 ? 129 : 1));
     __syncthreads();
     auto issue = [&](int it) {
         const int s = it % kProbeStages;
@@ -83,6 +84,25 @@ __global__ void __launch_bounds__(256, 1) row_gather_probe_kernel(const __grid_c
                 cp_async_16(st + sw128_offset(r, j), x + (int64_t)src * 128 + j * 16, 16u);
             }
             cp_async_arrive_noinc(&full[s]);
+            return;
+        }
+        if (mode == 4) {
+            if (tid == 0) mbar_arrive_expect_tx(&full[s], kProbeStage / 2);
+            __syncwarp();
+            if (warp == 0 && lane < 16) {
+                const int64_t r = rb + 4 * lane;
+                gather4_load(st + lane * 512, &tm, 0, rows[r % nlist], rows[(r + 1) % nlist], rows[(r + 2) % nlist],
+                             rows[(r + 3) % nlist], &full[s]);
+            }
+            if (warp >= 4) {
+                const int j = lane & 7, rsub = lane >> 3;
+                for (int q = 0; q < 4; ++q) {
+                    const int r = 64 + (warp - 4) * 16 + rsub + 4 * q;
+                    const int32_t src = rows[(rb + r) % nlist];
+                    cp_async_16(st + sw128_offset(r, j), x + (int64_t)src * 128 + j * 16, 16u);
+                }
+                cp_async_arrive_noinc(&full[s]);
+            }
             return;
         }
         int g0 = 0, gn = 0;
@@ -128,7 +148,7 @@ using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, vo
 
 extern "C" int fvgb_row_gather_probe(int32_t mode, const void *x, int64_t n_rows, const int32_t *rows, int32_t nlist,
                                      int32_t iters, int32_t *err_dev, int64_t *bytes, fvgb_stream_t stream) {
-    if (mode < 0 || mode > 3 || !x || n_rows < 1 || n_rows > INT32_MAX || !rows || nlist < 128 || iters < 1 ||
+    if (mode < 0 || mode > 4 || !x || n_rows < 1 || n_rows > INT32_MAX || !rows || nlist < 128 || iters < 1 ||
         !err_dev || !bytes || ((uintptr_t)x & 127))
         return FVGB_EINVAL;
     void *p = nullptr;

@@ -137,6 +137,22 @@ int fvgb_grid_leaf_scan(const int32_t *ijk, const int64_t *joffsets, int32_t num
 int fvgb_grid_index_build(const FvgbGrid *grid, const int32_t *leaf_ids, fvgb_stream_t stream);
 
 /*
+ * Coarse grid of floor(ijk / factor) (factor[a] in {1, 2, 4, 8}; num_grids <= 1024), built leaf by
+ * leaf: the fine leaves are grouped by the coarse leaf they fall in (one radix-sort key per fine
+ * leaf, not per voxel), each coarse leaf's mask is the OR of its fine leaves' voxels mapped down,
+ * and the coarse voxels are written leaf by leaf in bit order -- the same voxels in the same
+ * order as fvgb_ijk_sort_unique of floor(ijk / factor).  out_ijk and leaf_ids (capacity: the fine
+ * voxel count) receive the sorted voxels and their 1-based leaf ids (as fvgb_grid_leaf_scan);
+ * meta (device int64 [num_grids + 3], zeroed) the voxel offsets [0..num_grids], the leaf count and
+ * the voxel count.  The fine grid must have at least one leaf.  Replaces the coarse-grid paths of
+ * BuildGridForConv (src/fvdb/detail/ops/BuildGridForConv.cu:181-255, CoarseIjkForFineGrid.cu:19-41)
+ * and BuildCoarseGridFromFine.
+ */
+int fvgb_coarse_grid_workspace(int64_t num_fine_leaves, size_t *bytes);
+int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor[3], int32_t *out_ijk, int64_t *meta,
+                           int32_t *leaf_ids, void *workspace, size_t workspace_bytes, fvgb_stream_t stream);
+
+/*
  * Index of each query coordinate (query q belongs to grid b with joffsets[b] <= q <
  * joffsets[b+1]) in `grid`, or -1 where the grid has no voxel; global (cumulative != 0) or
  * per-grid index.  One leaf-hash probe per query.  Replaces GridBatch::ijk_to_index
@@ -489,7 +505,7 @@ int fvgb_ffma_probe(float *out, int64_t iters, int32_t blocks_per_sm, double *fl
  * 128B-swizzled shared-memory stage): one CTA of 256 threads per SM gathers `iters` stages of 128
  * rows (row indices rows[0..nlist), cycled) of x [n_rows, 128 B] into a 4-deep ring; mode 0/1/2:
  * TMA tile::gather4 issued by 1 thread / lane 0 of 8 warps / 32 lanes of one warp, mode 3:
- * cp.async by 8 warps.  *bytes (host) = bytes moved by the launch, which the caller times on
+ * cp.async by 8 warps, mode 4: half of each stage by gather4 and half by cp.async.  *bytes (host) = bytes moved by the launch, which the caller times on
  * `stream`; *err_dev (zeroed device int32) becomes FVGB_ETIMEOUT if a bounded wait gave up.  x
  * 128-byte aligned.  No counterpart in the reference. */
 int fvgb_row_gather_probe(int32_t mode, const void *x, int64_t n_rows, const int32_t *rows, int32_t nlist,

@@ -83,3 +83,29 @@ def test_large_grid_build_sorts_within_measured_bounds(cuda_device):
     ref, ref_off = orc.grid_from_ijk(ijk, off)
     assert np.array_equal(grid.ijk.jdata.cpu().numpy(), ref)
     assert np.array_equal(grid.joffsets.cpu().numpy(), ref_off)
+
+
+@pytest.mark.parametrize("factor", [(2, 2, 2), (4, 4, 4), (8, 8, 8), (2, 4, 1), (1, 8, 2)])
+def test_coarse_grid_by_leaves_equals_voxel_sort(cuda_device, factor):
+    """conv_grid(k = s) and coarsened_grid for power-of-two factors are built leaf by leaf
+    (fvgb_coarse_grid_build): exactly the voxels, order and offsets of the oracle's coarse grid
+    (floor(ijk / s) sorted voxel by voxel), for several grids, negative coordinates and sparse and
+    dense regions, and a working leaf table (ijk_to_index of every coarse voxel is its index)."""
+    import fvdb
+
+    from oracle import oracle as orc
+    from tests.helpers import random_sparse_ijk
+
+    parts = [random_sparse_ijk(6000, 48, 11, lo=-70), random_sparse_ijk(300, 9, 12, lo=5),
+             random_sparse_ijk(9000, 200, 13, lo=-1000)]
+    dense = np.stack(np.meshgrid(*[np.arange(-20, 20)] * 3, indexing="ij"), -1).reshape(-1, 3).astype(np.int32)
+    parts.append(dense)
+    grid = fvdb.GridBatch.from_ijk(fvdb.JaggedTensor([torch.from_numpy(p).to(cuda_device) for p in parts]))
+    ijk = grid.ijk.jdata.cpu().numpy()
+    off = grid.joffsets.cpu().numpy()
+    c_ijk, c_off = orc.conv_grid(ijk, off, factor, factor)
+    for coarse in (grid.conv_grid(factor, factor), grid.coarsened_grid(factor)):
+        assert np.array_equal(coarse.ijk.jdata.cpu().numpy(), c_ijk)
+        assert np.array_equal(coarse.joffsets.cpu().numpy(), c_off)
+        idx = coarse.ijk_to_index(coarse.ijk, cumulative=True).jdata.cpu().numpy()
+        assert np.array_equal(idx, np.arange(c_ijk.shape[0]))
