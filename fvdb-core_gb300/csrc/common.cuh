@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "../../include/fvdb_gb300.h"
 
 namespace fvgb {
@@ -21,6 +25,23 @@ void count_launches(int n);
 inline cudaStream_t as_stream(fvgb_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 // Streaming multiprocessors of the current device (cached per device).
 int device_sm_count();
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per (kernel, device) and size: the
+// attribute persists, and setting it before every launch costs host time on the launch path.
+template <typename F>
+inline cudaError_t set_dynamic_smem(F kern, int bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> done;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    const auto key = std::make_pair(reinterpret_cast<const void *>(kern), dev);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = done.find(key);
+    if (it != done.end() && it->second >= bytes) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done[key] = bytes;
+    return e;
+}
 
 constexpr int kLeafDim = 8;
 // find_leaf reads (origin, batch) of a leaf as one 16-byte load: leaves must stay 128 bytes.

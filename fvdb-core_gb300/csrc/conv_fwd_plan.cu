@@ -737,7 +737,7 @@ int launch_plan(PlanArgs a, cudaStream_t s) {
     const int smem = fixed + (a.resident ? (int)res_bytes : NSLOT * BN * kUnitBytes);
     if (smem > 227 * 1024) return FVGB_EINVAL;
     auto kern = conv_plan_fwd_kernel<BN, EB, PACK>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (set_dynamic_smem(kern, smem) != cudaSuccess)
         return launch_status();
     const int64_t grid = std::min<int64_t>(a.n_tiles, sm_count_p());
     kern<<<(unsigned)grid, kThreadsP, smem, s>>>(a);

@@ -582,7 +582,7 @@ int launch_fwd(FwdArgs a, cudaStream_t s) {
     a.stages = stages;
     const int smem = stages * stage + fixed;
     auto kern = conv_tc_fwd_kernel<BN, EB, PACK, U>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (set_dynamic_smem(kern, smem) != cudaSuccess)
         return launch_status();
     const int64_t grid = std::min<int64_t>(a.n_tiles, sm_count());
     kern<<<(unsigned)grid, kThreads, smem, s>>>(a);

@@ -447,7 +447,7 @@ int launch_wgrad(const CUtensorMap &dy_map, WgArgs a, int64_t blocks, int64_t ch
     a.stages = stages;
     const int smem = stages * kA + 2 * kDy + extra;
     auto kern = conv_tc_wgrad_kernel<BN>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (set_dynamic_smem(kern, smem) != cudaSuccess)
         return launch_status();
     kern<<<dim3((unsigned)blocks, (unsigned)chunks), kWgThreads, smem, s>>>(dy_map, a);
     return launch_status();

@@ -602,15 +602,17 @@ size_t coarse_ws_layout(int64_t nl, CoarseWs *w, char *base) {
     return off;
 }
 
-// key of fine leaf l: (grid << 54) | (order key of its coarse leaf's origin >> 9)
-__global__ void coarse_keys_kernel(const FvgbLeaf *__restrict__ leaves, int64_t nl, int3 sh,
-                                   uint64_t *__restrict__ keys, int32_t *__restrict__ vals) {
+// key of fine leaf l: (grid << vb) | ((order key of its coarse leaf's origin & low_mask) >> 9); the
+// bits above low_mask agree for every coarse voxel of the bounding box, so dropping them keeps the
+// order and shortens the sort
+__global__ void coarse_keys_kernel(const FvgbLeaf *__restrict__ leaves, int64_t nl, int3 sh, uint64_t low_mask,
+                                   int vb, uint64_t *__restrict__ keys, int32_t *__restrict__ vals) {
     const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= nl) return;
     const FvgbLeaf &lf = leaves[l];
     const int32_t cx = (lf.origin[0] >> (sh.x + 3)) << 3, cy = (lf.origin[1] >> (sh.y + 3)) << 3,
                   cz = (lf.origin[2] >> (sh.z + 3)) << 3;
-    keys[l] = ((uint64_t)lf.batch << 54) | (order_key(cx, cy, cz) >> 9);
+    keys[l] = ((uint64_t)lf.batch << vb) | ((order_key(cx, cy, cz) & low_mask) >> 9);
     vals[l] = (int32_t)l;
 }
 
@@ -716,9 +718,9 @@ extern "C" int fvgb_coarse_grid_workspace(int64_t num_fine_leaves, size_t *bytes
     return FVGB_OK;
 }
 
-extern "C" int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor[3], int32_t *out_ijk,
-                                      int64_t *meta, int32_t *leaf_ids, void *workspace, size_t workspace_bytes,
-                                      fvgb_stream_t stream) {
+extern "C" int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor[3], const int32_t *box_lo,
+                                      const int32_t *box_hi, int32_t *out_ijk, int64_t *meta, int32_t *leaf_ids,
+                                      void *workspace, size_t workspace_bytes, fvgb_stream_t stream) {
     if (!fine || !factor || !meta) return FVGB_EINVAL;
     if (fine->num_grids < 1 || fine->num_grids > kCoarseMaxGrids) return FVGB_EINVAL;
     int sh[3];
@@ -739,10 +741,23 @@ extern "C" int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor
     CoarseWs w;
     coarse_ws_layout(nl, &w, base);
     const int3 shv = make_int3(sh[0], sh[1], sh[2]);
+    // key bits: the order-key bits that vary inside the coarse bounding box (all 63 without one),
+    // less the 9 leaf bits, under the grid index
+    int end_bit = 63;
+    if (box_lo && box_hi) {
+        for (int a = 0; a < 3; ++a)
+            if (box_lo[a] > box_hi[a]) return FVGB_EINVAL;
+        end_bit = order_key_end_bit(box_lo, box_hi);
+    }
+    const int vb = end_bit > 9 ? end_bit - 9 : 0;
+    const uint64_t low_mask = end_bit >= 63 ? ~0ull : ((1ull << end_bit) - 1ull);
+    int grid_bits = 0;
+    while ((1 << grid_bits) < fine->num_grids) ++grid_bits;
+    const int sort_bits = std::max(1, vb + grid_bits);
     if (cudaMemsetAsync(w.cmask, 0, (size_t)nl * 64, s) != cudaSuccess) return launch_status();
-    coarse_keys_kernel<<<blocks_for(nl), kThreads, 0, s>>>(fine->leaves, nl, shv, w.keys_a, w.vals_a);
+    coarse_keys_kernel<<<blocks_for(nl), kThreads, 0, s>>>(fine->leaves, nl, shv, low_mask, vb, w.keys_a, w.vals_a);
     size_t tb = w.cub_bytes;
-    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.vals_a, w.vals_b, (int)nl, 0, 64, s);
+    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.vals_a, w.vals_b, (int)nl, 0, sort_bits, s);
     coarse_flags_kernel<<<blocks_for(nl), kThreads, 0, s>>>(w.keys_b, nl, w.count);
     tb = w.cub_bytes;
     cub::DeviceScan::InclusiveSum(w.cub_tmp, tb, w.count, w.cid, (int)nl, s);

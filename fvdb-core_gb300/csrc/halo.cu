@@ -329,7 +329,7 @@ template <typename T>
 int launch_halo_fwd(const FvgbGrid &g, const void *x, int64_t ldx, int32_t Cin, const void *w, int32_t Cout,
                     int32_t mirror, void *y, int64_t ldy, cudaStream_t s) {
     constexpr int smem = halo_smem_bytes<T>();
-    if (cudaFuncSetAttribute(halo_fwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (set_dynamic_smem(halo_fwd_kernel<T>, smem) != cudaSuccess)
         return launch_status();
     const unsigned blocks = (unsigned)std::min<int64_t>(g.num_leaves, (int64_t)device_sm_count() * 8);
     halo_fwd_kernel<T><<<blocks, kHT, smem, s>>>(g, (const T *)x, ldx, Cin, (const T *)w, Cout, mirror, (T *)y, ldy);

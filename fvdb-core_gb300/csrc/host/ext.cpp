@@ -11,10 +11,13 @@
 // current torch stream.  Errors map to ValueError / TypeError / RuntimeError exactly where the
 // reference uses TORCH_CHECK_VALUE / TORCH_CHECK_TYPE / TORCH_CHECK.
 #include <ATen/cuda/CUDAContext.h>
+#include <ATen/cuda/CUDAEvent.h>
 #include <c10/cuda/CUDAGuard.h>
 #include <torch/extension.h>
 
+#include <list>
 #include <map>
+#include <mutex>
 #include <optional>
 #include <string>
 #include <vector>
@@ -103,6 +106,9 @@ struct GridImpl {
     Tensor origins;        // float64 [B,3] cpu
     Tensor jidx_cache;
     int32_t box_lo[3] = {0, 0, 0}, box_hi[3] = {-1, -1, -1};  // bounding box of ijk (empty if N == 0)
+    // recorded on the building stream after the last kernel of the build: work on another stream
+    // that reads the grid waits for this, not for everything queued after it
+    std::shared_ptr<at::cuda::CUDAEvent> ready;
 
     FvgbGrid view() const {
         FvgbGrid g;
@@ -231,6 +237,8 @@ GridPtr build_grid(const Tensor &ijk_in, const Tensor &joff_in, const Tensor &vs
     g->hash = torch::empty({g->cap}, i32);
     FvgbGrid v = g->view();
     check_status(fvgb_grid_index_build(&v, leaf_ids.data_ptr<int32_t>(), s), "grid build (index)");
+    g->ready = std::make_shared<at::cuda::CUDAEvent>();
+    g->ready->record(at::cuda::getCurrentCUDAStream(dev.index()));
     return g;
 }
 
@@ -260,6 +268,17 @@ GridPtr grid_from_points(const Tensor &points, const Tensor &joffsets, const Ten
 // Coarse grid floor(ijk / f) of a grid, built leaf by leaf (fvgb_coarse_grid_build: one sort
 // key per fine leaf instead of one per voxel; the same voxels in the same order as sorting the
 // coarsened voxels).  f per axis in {1, 2, 4, 8}; lo/hi: bounds of the coarse voxels.
+// A stream of the library's own per device, for builds whose counts the host must read: the host
+// then waits for the build alone, not for the convolutions queued on the caller's stream before it.
+c10::cuda::CUDAStream build_stream(c10::DeviceIndex dev) {
+    static std::mutex mu;
+    static std::map<int, c10::cuda::CUDAStream> streams;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = streams.find(dev);
+    if (it == streams.end()) it = streams.emplace(dev, c10::cuda::getStreamFromPool(false, dev)).first;
+    return it->second;
+}
+
 GridPtr build_coarse_by_leaves(const GridPtr &g, const Vec3 &f, const int32_t lo[3], const int32_t hi[3]) {
     auto dev = g->device();
     const int64_t B = g->B;
@@ -268,23 +287,43 @@ GridPtr build_coarse_by_leaves(const GridPtr &g, const Vec3 &f, const int32_t lo
     c->voxel_sizes = g->voxel_sizes.clone();
     c->origins = g->origins.clone();
     auto i32 = torch::dtype(torch::kInt32).device(dev);
-    Tensor out_ijk = torch::empty({std::max<int64_t>(g->N, 1), 3}, i32);
-    Tensor leaf_ids = torch::empty({std::max<int64_t>(g->N, 1)}, i32);
-    Tensor meta = torch::zeros({B + 4}, torch::dtype(torch::kInt64).device(dev));
-    size_t wsb = 0;
-    check_status(fvgb_coarse_grid_workspace(g->L, &wsb), "coarse grid (workspace)");
-    Tensor ws = workspace(wsb, dev);
-    FvgbGrid fv = g->view();
-    auto s = cur_stream();
-    check_status(fvgb_coarse_grid_build(&fv, f.v, out_ijk.data_ptr<int32_t>(), meta.data_ptr<int64_t>(),
-                                        leaf_ids.data_ptr<int32_t>(), ws.data_ptr(), ws.numel(), s),
-                 "coarse grid");
+    // The build runs on the library's build stream once the fine grid is complete (its ready
+    // event), so the one host read of the counts does not wait for work queued on the caller's
+    // stream (e.g. the previous step's convolutions); buffers are allocated for that stream and
+    // handed to the caller's stream afterwards.
+    auto main = at::cuda::getCurrentCUDAStream(dev.index());
+    auto side = build_stream(dev.index());
+    if (g->ready) g->ready->block(side);
+    else {
+        at::cuda::CUDAEvent e;
+        e.record(main);
+        e.block(side);
+    }
+    Tensor out_ijk, leaf_ids, meta;
     int64_t *h = pinned_meta(dev.index(), (size_t)(B + 4));
-    cudaStream_t cs = reinterpret_cast<cudaStream_t>(s);
-    TORCH_CHECK(cudaMemcpyAsync(h, meta.data_ptr<int64_t>(), (B + 4) * sizeof(int64_t), cudaMemcpyDeviceToHost, cs) ==
-                        cudaSuccess &&
-                    cudaStreamSynchronize(cs) == cudaSuccess,
-                "coarse grid: reading the counts failed");
+    {
+        c10::cuda::CUDAStreamGuard sg(side);
+        out_ijk = torch::empty({std::max<int64_t>(g->N, 1), 3}, i32);
+        leaf_ids = torch::empty({std::max<int64_t>(g->N, 1)}, i32);
+        meta = torch::zeros({B + 4}, torch::dtype(torch::kInt64).device(dev));
+        size_t wsb = 0;
+        check_status(fvgb_coarse_grid_workspace(g->L, &wsb), "coarse grid (workspace)");
+        Tensor ws = workspace(wsb, dev);
+        FvgbGrid fv = g->view();
+        cudaStream_t cs = side.stream();
+        check_status(fvgb_coarse_grid_build(&fv, f.v, lo, hi, out_ijk.data_ptr<int32_t>(), meta.data_ptr<int64_t>(),
+                                            leaf_ids.data_ptr<int32_t>(), ws.data_ptr(), ws.numel(), cs),
+                     "coarse grid");
+        TORCH_CHECK(cudaMemcpyAsync(h, meta.data_ptr<int64_t>(), (B + 4) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                    cs) == cudaSuccess &&
+                        cudaStreamSynchronize(cs) == cudaSuccess,
+                    "coarse grid: reading the counts failed");
+    }
+    // the build stream is idle again; its buffers live on in the caller's stream
+    out_ijk.record_stream(main);
+    leaf_ids.record_stream(main);
+    meta.record_stream(main);
+    auto s = cur_stream();
     for (int a = 0; a < 3; ++a) {
         c->box_lo[a] = lo[a];
         c->box_hi[a] = hi[a];
@@ -300,6 +339,8 @@ GridPtr build_coarse_by_leaves(const GridPtr &g, const Vec3 &f, const int32_t lo
     c->hash = torch::empty({c->cap}, i32);
     FvgbGrid v = c->view();
     check_status(fvgb_grid_index_build(&v, leaf_ids.data_ptr<int32_t>(), s), "coarse grid (index)");
+    c->ready = std::make_shared<at::cuda::CUDAEvent>();
+    c->ready->record(main);
     return c;
 }
 
@@ -724,6 +765,69 @@ bool use_tensor_cores(const Tensor &x, int64_t cin, int64_t cout) {
            x.stride(0) % 8 == 0;
 }
 
+// Derived weight tensors, cached per source tensor: the [K, Cin, Cout] view / copy of a 5-D
+// weight (reshaping a permuted weight copies it) and the packed tensor-core image of a
+// [K, Cin, Cout] weight.  An entry is valid while its source tensor's storage is alive and its
+// version counter unchanged (an in-place update, e.g. an optimizer step, makes a new entry), so
+// repeated convolutions with the same weights (inference, layers of a serving stack) skip the
+// copy and the packing launch.
+struct DerivedKey {
+    const void *storage;
+    int64_t offset;
+    std::vector<int64_t> sizes, strides;
+    c10::ScalarType dtype;
+    int64_t version;
+    int tag;  // what is derived: 0/1 = [K, Cin, Cout] (not transposed / transposed), 2/3 = packed (W / W^T)
+    bool operator==(const DerivedKey &o) const {
+        return storage == o.storage && offset == o.offset && sizes == o.sizes && strides == o.strides &&
+               dtype == o.dtype && version == o.version && tag == o.tag;
+    }
+};
+struct DerivedEntry {
+    DerivedKey key;
+    c10::weak_intrusive_ptr<c10::StorageImpl> alive;
+    Tensor value;
+};
+
+DerivedKey derived_key(const Tensor &t, int tag) {
+    return DerivedKey{t.storage().unsafeGetStorageImpl(), t.storage_offset(), t.sizes().vec(), t.strides().vec(),
+                      t.scalar_type(), (int64_t)t.unsafeGetTensorImpl()->version_counter().current_version(), tag};
+}
+
+std::mutex g_derived_mu;
+std::list<DerivedEntry> g_derived;  // most recently used first
+constexpr size_t kDerivedMax = 64;
+
+std::optional<Tensor> derived_get(const Tensor &src, int tag) {
+    const DerivedKey k = derived_key(src, tag);
+    std::lock_guard<std::mutex> lock(g_derived_mu);
+    for (auto it = g_derived.begin(); it != g_derived.end();) {
+        auto live = it->alive.lock();
+        if (!live) {  // the source storage is gone: drop the entry
+            it = g_derived.erase(it);
+            continue;
+        }
+        if (it->key == k && live.get() == src.storage().unsafeGetStorageImpl()) {
+            g_derived.splice(g_derived.begin(), g_derived, it);
+            return g_derived.front().value;
+        }
+        ++it;
+    }
+    return std::nullopt;
+}
+
+void derived_put(const Tensor &src, int tag, const Tensor &value) {
+    DerivedEntry e{derived_key(src, tag), c10::weak_intrusive_ptr<c10::StorageImpl>(src.storage().getWeakStorageImpl()),
+                   value};
+    std::lock_guard<std::mutex> lock(g_derived_mu);
+    // an older version of the same source is stale for good: drop it
+    g_derived.remove_if([&](const DerivedEntry &o) {
+        return o.key.storage == e.key.storage && o.key.offset == e.key.offset && o.key.tag == e.key.tag;
+    });
+    g_derived.push_front(std::move(e));
+    while (g_derived.size() > kDerivedMax) g_derived.pop_back();
+}
+
 // y[m] = sum_k x[map[m,k]] W[k]   for the first n_out rows of map
 // bias (optional, [cout]): added in the tensor-core epilogue, else after the contraction.
 // pack / map_t (optional): the pack info that owns `map` and whether `map` is its transposed map;
@@ -744,12 +848,20 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
     const int32_t dt = fvgb_dtype(x);
     auto s = cur_stream();
     if (use_tensor_cores(x, cin, cout)) {
-        size_t wb = 0;
-        check_status(fvgb_tc_weight_bytes(FVGB_BF16, K, (int32_t)cin, (int32_t)cout, &wb), "weight pack size");
-        Tensor packed = torch::empty({(int64_t)wb}, torch::dtype(torch::kUInt8).device(x.device()));
-        check_status(fvgb_tc_pack_weights(FVGB_BF16, w.data_ptr(), K, (int32_t)cin, (int32_t)cout, wsk, wsci, wsco,
-                                          packed.data_ptr(), wb, s),
-                     "weight pack");
+        const int tag = transpose_w ? 3 : 2;
+        std::optional<Tensor> cached = derived_get(Wkio, tag);
+        Tensor packed;
+        if (cached && cached->device() == x.device()) {
+            packed = *cached;
+        } else {
+            size_t wb = 0;
+            check_status(fvgb_tc_weight_bytes(FVGB_BF16, K, (int32_t)cin, (int32_t)cout, &wb), "weight pack size");
+            packed = torch::empty({(int64_t)wb}, torch::dtype(torch::kUInt8).device(x.device()));
+            check_status(fvgb_tc_pack_weights(FVGB_BF16, w.data_ptr(), K, (int32_t)cin, (int32_t)cout, wsk, wsci,
+                                              wsco, packed.data_ptr(), wb, s),
+                         "weight pack");
+            if (Wkio.scalar_type() == torch::kBFloat16) derived_put(Wkio, tag, packed);
+        }
         const uint32_t *tm = tile_mask ? reinterpret_cast<const uint32_t *>(tile_mask->data_ptr<int32_t>()) : nullptr;
         Tensor b32;
         if (bias) b32 = bias->to(torch::kFloat32).contiguous();
@@ -877,14 +989,26 @@ std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr
                           ") to equal input channels of features: ", x.size(1));
         cout = weights.size(0);
         cin = weights.size(1);
-        Wkio = weights.permute({4, 3, 2, 1, 0}).reshape({-1, cin, cout});
+        if (auto c = derived_get(weights, 0)) {
+            Wkio = *c;
+        } else {
+            Wkio = weights.permute({4, 3, 2, 1, 0}).reshape({-1, cin, cout});
+            // a copy is worth keeping; a view is free to make again (and must not pin the weights)
+            if (!Wkio.is_alias_of(weights)) derived_put(weights, 0, Wkio);
+        }
     } else {
         TORCH_CHECK_VALUE(x.size(0) == n_tgt, "The number of input features must match the number of voxels");
         TORCH_CHECK_VALUE(weights.size(0) == x.size(1), "Expected input channels of kernels (", weights.size(0),
                           ") to equal input channels of features: ", x.size(1));
         cin = weights.size(0);
         cout = weights.size(1);
-        Wkio = weights.permute({4, 3, 2, 0, 1}).reshape({-1, cin, cout});
+        if (auto c = derived_get(weights, 1)) {
+            Wkio = *c;
+        } else {
+            Wkio = weights.permute({4, 3, 2, 0, 1}).reshape({-1, cin, cout});
+            // a copy is worth keeping; a view is free to make again (and must not pin the weights)
+            if (!Wkio.is_alias_of(weights)) derived_put(weights, 1, Wkio);
+        }
     }
     if (bias) {
         TORCH_CHECK_VALUE(bias->dim() == 1 && bias->size(0) == cout, "bias must have shape (", cout, ",)");

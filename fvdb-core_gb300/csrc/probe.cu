@@ -165,7 +165,7 @@ extern "C" int fvgb_row_gather_probe(int32_t mode, const void *x, int64_t n_rows
                                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return FVGB_EINVAL;
     const int smem = kProbeStages * kProbeStage + 1024 + 64;
-    if (cudaFuncSetAttribute(row_gather_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (set_dynamic_smem(row_gather_probe_kernel, smem) != cudaSuccess)
         return launch_status();
     const int blocks = device_sm_count();
     row_gather_probe_kernel<<<blocks, 256, smem, as_stream(stream)>>>(tm, (const uint8_t *)x, rows, nlist, iters, mode,

@@ -144,13 +144,16 @@ int fvgb_grid_index_build(const FvgbGrid *grid, const int32_t *leaf_ids, fvgb_st
  * order as fvgb_ijk_sort_unique of floor(ijk / factor).  out_ijk and leaf_ids (capacity: the fine
  * voxel count) receive the sorted voxels and their 1-based leaf ids (as fvgb_grid_leaf_scan);
  * meta (device int64 [num_grids + 3], zeroed) the voxel offsets [0..num_grids], the leaf count and
- * the voxel count.  The fine grid must have at least one leaf.  Replaces the coarse-grid paths of
+ * the voxel count.  box_lo/box_hi (optional, host int32[3]): bounds of the coarse voxels, which
+ * shorten the sort to the key bits that vary.  The fine grid must have at least one leaf.
+ * Replaces the coarse-grid paths of
  * BuildGridForConv (src/fvdb/detail/ops/BuildGridForConv.cu:181-255, CoarseIjkForFineGrid.cu:19-41)
  * and BuildCoarseGridFromFine.
  */
 int fvgb_coarse_grid_workspace(int64_t num_fine_leaves, size_t *bytes);
-int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor[3], int32_t *out_ijk, int64_t *meta,
-                           int32_t *leaf_ids, void *workspace, size_t workspace_bytes, fvgb_stream_t stream);
+int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor[3], const int32_t *box_lo, const int32_t *box_hi,
+                           int32_t *out_ijk, int64_t *meta, int32_t *leaf_ids, void *workspace, size_t workspace_bytes,
+                           fvgb_stream_t stream);
 
 /*
  * Index of each query coordinate (query q belongs to grid b with joffsets[b] <= q <
