@@ -268,14 +268,16 @@ GridPtr grid_from_points(const Tensor &points, const Tensor &joffsets, const Ten
 // Coarse grid floor(ijk / f) of a grid, built leaf by leaf (fvgb_coarse_grid_build: one sort
 // key per fine leaf instead of one per voxel; the same voxels in the same order as sorting the
 // coarsened voxels).  f per axis in {1, 2, 4, 8}; lo/hi: bounds of the coarse voxels.
-// A stream of the library's own per device, for builds whose counts the host must read: the host
-// then waits for the build alone, not for the convolutions queued on the caller's stream before it.
+// A high-priority stream of the library's own per device, for builds whose counts the host must
+// read: the host then waits for the build alone, not for the convolutions queued on the caller's
+// stream before it, and the build's small CTAs are scheduled into the room the running
+// persistent convolution CTAs leave on each SM instead of queueing behind them.
 c10::cuda::CUDAStream build_stream(c10::DeviceIndex dev) {
     static std::mutex mu;
     static std::map<int, c10::cuda::CUDAStream> streams;
     std::lock_guard<std::mutex> lock(mu);
     auto it = streams.find(dev);
-    if (it == streams.end()) it = streams.emplace(dev, c10::cuda::getStreamFromPool(false, dev)).first;
+    if (it == streams.end()) it = streams.emplace(dev, c10::cuda::getStreamFromPool(true, dev)).first;
     return it->second;
 }
 
