@@ -149,11 +149,10 @@ def useful_flops(p1, p2, cin1=32, cout1=64, cin2=64, cout2=64) -> tuple[float, i
     return 2.0 * (P1 * cin1 * cout1 + P2 * cin2 * cout2), P1, P2
 
 
-# DRAM bytes (read + write) of one layer-1 contraction launch per voxel, from an ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum) of one launch on the same workload generator
-# at 500k points per grid: (142.95 + 70.46) MB over 829,865 voxels; traffic grows with the
-# voxel count.
-L1_DRAM_BYTES_PER_VOXEL = (142.949e6 + 70.459e6) / 829_865
+# DRAM bytes (read + write) of one layer-1 contraction launch per voxel, from an ncu capture of
+# one launch on the same workload generator at 1M points per grid (988,678 voxels): DRAM
+# throughput 781.7 GB/s over the 335.26 us launch = 262.1 MB; traffic grows with the voxel count.
+L1_DRAM_BYTES_PER_VOXEL = 781.685597e9 * 335.264e-6 / 988_678
 
 
 def kernel_only_l1(lib, p1, x: torch.Tensor, w1: torch.Tensor, launches: int) -> dict:
