@@ -381,14 +381,23 @@ def run_gpu(args) -> None:
         h2d = ijk_host.numel() * 4 + x_host.numel() * 2 + off_host.numel() * 8
         out_host = None  # pinned result buffer, allocated once like a serving loop would
 
+        copy_stream = torch.cuda.Stream(device=dev)
+
         def e2e_step():
             nonlocal out_host
             ijk_d = ijk_host.to(dev, non_blocking=True)
-            x_d = x_host.to(dev, non_blocking=True)
+            # the features travel on a copy stream while the grid is built from the coordinates
+            copy_stream.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(copy_stream):
+                x_d = x_host.to(dev, non_blocking=True)
+            x_ready = torch.cuda.Event()
+            x_ready.record(copy_stream)
             grid_e = fvdb.GridBatch.from_ijk(fvdb.JaggedTensor.from_data_and_offsets(ijk_d, off_host.to(dev, non_blocking=True)))
             # the voxel order of the built grid is the grid's own: features are given per input row,
             # so they are reordered through ijk_to_index as a user would
             idx = grid_e.ijk_to_index(fvdb.JaggedTensor.from_data_and_offsets(ijk_d, off_host.to(dev)), cumulative=True).jdata
+            torch.cuda.current_stream().wait_event(x_ready)
+            x_d.record_stream(torch.cuda.current_stream())
             x_sorted = torch.empty_like(x_d)
             x_sorted[idx] = x_d
             y_e, *_ = model.forward(grid_e, x_sorted)

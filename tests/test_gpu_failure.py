@@ -41,3 +41,34 @@ def test_bounded_wait_reports_timeout_and_context_survives(cuda_device):
     torch.cuda.synchronize()
     fvdb._lib.load().check_device_errors(cuda_device)
     assert y.shape == (grid.total_voxels, 64) and bool(torch.isfinite(y.float()).all())
+
+
+def test_measurement_probes_run(cuda_device):
+    """The FFMA and row-gather probes launch, finish without a timeout and report their work."""
+    import ctypes
+
+    from fvdb import _lib
+
+    lib = _lib.cdll()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = torch.zeros(2, device=cuda_device)
+    flops = ctypes.c_double(0.0)
+    assert lib.fvgb_ffma_probe(ctypes.c_void_p(out.data_ptr()), ctypes.c_int64(64), 1, ctypes.byref(flops), stream) == 0
+    torch.cuda.synchronize()
+    assert flops.value > 0
+    n = 4096
+    x = torch.zeros(n, 64, device=cuda_device, dtype=torch.bfloat16)
+    rows = torch.randint(0, n, (1024,), device=cuda_device, dtype=torch.int32)
+    err = torch.zeros(1, device=cuda_device, dtype=torch.int32)
+    nbytes = ctypes.c_int64(0)
+    for mode in range(5):
+        assert lib.fvgb_row_gather_probe(mode, ctypes.c_void_p(x.data_ptr()), ctypes.c_int64(n),
+                                         ctypes.c_void_p(rows.data_ptr()), rows.numel(), 8,
+                                         ctypes.c_void_p(err.data_ptr()), ctypes.byref(nbytes), stream) == 0
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0 and nbytes.value > 0
+    # argument checks: unknown mode, too few row indices
+    assert lib.fvgb_row_gather_probe(5, ctypes.c_void_p(x.data_ptr()), ctypes.c_int64(n), ctypes.c_void_p(rows.data_ptr()),
+                                     rows.numel(), 8, ctypes.c_void_p(err.data_ptr()), ctypes.byref(nbytes), stream) == 1
+    assert lib.fvgb_row_gather_probe(3, ctypes.c_void_p(x.data_ptr()), ctypes.c_int64(n), ctypes.c_void_p(rows.data_ptr()),
+                                     64, 8, ctypes.c_void_p(err.data_ptr()), ctypes.byref(nbytes), stream) == 1
