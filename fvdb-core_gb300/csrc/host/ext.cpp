@@ -602,7 +602,8 @@ std::optional<RowOrder> pack_row_order(PackPtr p, bool transposed) {
 // 0.19 ms for 1.08M rows x 27 (a sort and a permuted copy of the map), so the first tensor-core
 // contraction over a map runs in index order and the order serves the second and later ones
 // (training re-uses every map for forward and data gradient).  The CUDA-core forms use the order
-// from the first call: it saves them far more than it costs (C2 layer 1 FP32: 3.1 -> 2.0 ms).
+// from the first call on large maps: it saves them far more than it costs (C2 layer 1 FP32:
+// 3.1 -> 2.0 ms).
 std::optional<RowOrder> pack_row_order_if_reused(PackPtr p, bool transposed) {
     const int d = transposed ? 1 : 0;
     if (!p->order_rows[d] && ++p->order_requests[d] < 2) return std::nullopt;
@@ -902,7 +903,11 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
                      "sparse conv forward (tensor cores)");
         return y;
     } else if (dt == FVGB_F32 || dt == FVGB_F64) {
-        const auto order = pack ? pack_row_order(pack, map_t) : std::nullopt;
+        // large maps take the row order at once (C2 layer 1 FP32: 3.1 -> 1.9 ms for a 0.23 ms
+        // build); small ones only once reused, where the build's launches would dominate
+        const auto order = !pack ? std::nullopt
+                                 : (n_out >= (int64_t)1 << 16 ? pack_row_order(pack, map_t)
+                                                              : pack_row_order_if_reused(pack, map_t));
         const Tensor &m_used = order ? order->map : map;
         check_status(fvgb_conv_fwd_simt_rows(dt, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
                                              m_used.data_ptr<int32_t>(), n_out, (int32_t)K, m_used.stride(0),
