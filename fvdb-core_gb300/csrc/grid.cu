@@ -580,6 +580,9 @@ size_t coarse_ws_layout(int64_t nl, CoarseWs *w, char *base) {
     cub::DeviceRadixSort::SortPairs(nullptr, c, (uint64_t *)nullptr, (uint64_t *)nullptr, (int32_t *)nullptr,
                                     (int32_t *)nullptr, (int)nl, 0, 64);
     cub_bytes = c;
+    cub::DeviceRadixSort::SortPairs(nullptr, c, (uint32_t *)nullptr, (uint32_t *)nullptr, (int32_t *)nullptr,
+                                    (int32_t *)nullptr, (int)nl, 0, 32);
+    if (c > cub_bytes) cub_bytes = c;
     cub::DeviceScan::InclusiveSum(nullptr, c, (int32_t *)nullptr, (int32_t *)nullptr, (int)nl);
     if (c > cub_bytes) cub_bytes = c;
     cub::DeviceScan::ExclusiveSum(nullptr, c, (int32_t *)nullptr, (int32_t *)nullptr, (int)nl + 1);
@@ -616,10 +619,17 @@ __global__ void coarse_keys_kernel(const FvgbLeaf *__restrict__ leaves, int64_t 
     vals[l] = (int32_t)l;
 }
 
-__global__ void coarse_flags_kernel(const uint64_t *__restrict__ keys, int64_t nl, int32_t *__restrict__ flags) {
+template <typename Key>
+__global__ void coarse_flags_kernel(const Key *__restrict__ keys, int64_t nl, int32_t *__restrict__ flags) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nl) return;
     flags[p] = (p == 0 || keys[p] != keys[p - 1]) ? 1 : 0;
+}
+
+// keys that fit 32 bits, narrowed for a sort with half the traffic and a smaller footprint
+__global__ void narrow_keys_kernel(const uint64_t *__restrict__ k64, int64_t nl, uint32_t *__restrict__ k32) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < nl) k32[p] = (uint32_t)k64[p];
 }
 
 // warp per sorted fine leaf: OR its voxels, mapped down, into its coarse leaf's mask
@@ -757,8 +767,21 @@ extern "C" int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor
     if (cudaMemsetAsync(w.cmask, 0, (size_t)nl * 64, s) != cudaSuccess) return launch_status();
     coarse_keys_kernel<<<blocks_for(nl), kThreads, 0, s>>>(fine->leaves, nl, shv, low_mask, vb, w.keys_a, w.vals_a);
     size_t tb = w.cub_bytes;
-    cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.vals_a, w.vals_b, (int)nl, 0, sort_bits, s);
-    coarse_flags_kernel<<<blocks_for(nl), kThreads, 0, s>>>(w.keys_b, nl, w.count);
+    int launched = 6;  // keys, flags, mask, count, emit, offsets (+ narrow)
+    if (sort_bits <= 32) {
+        // 32-bit keys: the sort's kernels need less shared memory, so they also fit on SMs that a
+        // running convolution kernel occupies
+        uint32_t *k32a = reinterpret_cast<uint32_t *>(w.keys_b);  // the narrowed keys
+        uint32_t *k32b = reinterpret_cast<uint32_t *>(w.keys_a);  // sorted: keys_a is free once narrowed
+        narrow_keys_kernel<<<blocks_for(nl), kThreads, 0, s>>>(w.keys_a, nl, k32a);
+        cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, k32a, k32b, w.vals_a, w.vals_b, (int)nl, 0, sort_bits, s);
+        coarse_flags_kernel<uint32_t><<<blocks_for(nl), kThreads, 0, s>>>(k32b, nl, w.count);
+        ++launched;
+    } else {
+        cub::DeviceRadixSort::SortPairs(w.cub_tmp, tb, w.keys_a, w.keys_b, w.vals_a, w.vals_b, (int)nl, 0, sort_bits,
+                                        s);
+        coarse_flags_kernel<uint64_t><<<blocks_for(nl), kThreads, 0, s>>>(w.keys_b, nl, w.count);
+    }
     tb = w.cub_bytes;
     cub::DeviceScan::InclusiveSum(w.cub_tmp, tb, w.count, w.cid, (int)nl, s);
     coarse_mask_kernel<<<(unsigned)ceil_div(nl, 8), 256, 0, s>>>(fine->leaves, nl, shv, w.vals_b, w.cid, w.cmask,
@@ -770,6 +793,6 @@ extern "C" int fvgb_coarse_grid_build(const FvgbGrid *fine, const int32_t factor
                                                                 leaf_ids);
     coarse_offsets_kernel<<<(unsigned)ceil_div(fine->num_grids + 1, kThreads), kThreads, 0, s>>>(
         w.corig, w.cid, w.base, nl, fine->num_grids, meta);
-    count_launches(7);
+    count_launches(launched);  // CUB's own launches are not counted
     return launch_status();
 }
