@@ -15,6 +15,7 @@
 #include <c10/cuda/CUDAGuard.h>
 #include <torch/extension.h>
 
+#include <atomic>
 #include <list>
 #include <map>
 #include <mutex>
@@ -110,7 +111,32 @@ struct GridImpl {
     // that reads the grid waits for this, not for everything queued after it
     std::shared_ptr<at::cuda::CUDAEvent> ready;
 
+    // A grid whose counts are still on their way to the host (a coarse grid built on the build
+    // stream): the build is enqueued and resolve() completes the grid at its first use, so the
+    // caller's stream can be fed meanwhile (e.g. the next layer's convolution).  Until then N and
+    // L are -1, and every accessor of the counts, tensors or view resolves first.
+    struct PendingBuild {
+        at::cuda::CUDAEvent counted;  // on the build stream, after the counts' copy to the host
+        Tensor meta_host;             // pinned int64 [B + 4]
+        Tensor out_ijk, leaf_ids, meta;
+        // the counts' copy into meta_host must land before the pinned block can be reused
+        ~PendingBuild() {
+            try {
+                counted.synchronize();
+            } catch (...) {
+            }
+        }
+    };
+    std::unique_ptr<PendingBuild> pending;
+    std::atomic<bool> is_pending{false};
+    std::mutex resolve_mu;
+    void resolve() const;
+
     FvgbGrid view() const {
+        resolve();
+        return view_unchecked();
+    }
+    FvgbGrid view_unchecked() const {
         FvgbGrid g;
         g.num_grids = (int32_t)B;
         g.reserved = 0;
@@ -126,6 +152,11 @@ struct GridImpl {
     torch::Device device() const { return joffsets.device(); }
 };
 using GridPtr = std::shared_ptr<GridImpl>;
+
+const GridPtr &R(const GridPtr &g) {
+    if (g) g->resolve();
+    return g;
+}
 
 Tensor per_grid_vec(const Tensor &t, int64_t B, const char *name) {
     Tensor v = t.to(torch::kFloat64).cpu();
@@ -288,11 +319,15 @@ GridPtr build_coarse_by_leaves(const GridPtr &g, const Vec3 &f, const int32_t lo
     c->B = B;
     c->voxel_sizes = g->voxel_sizes.clone();
     c->origins = g->origins.clone();
+    for (int a = 0; a < 3; ++a) {
+        c->box_lo[a] = lo[a];
+        c->box_hi[a] = hi[a];
+    }
     auto i32 = torch::dtype(torch::kInt32).device(dev);
     // The build runs on the library's build stream once the fine grid is complete (its ready
-    // event), so the one host read of the counts does not wait for work queued on the caller's
-    // stream (e.g. the previous step's convolutions); buffers are allocated for that stream and
-    // handed to the caller's stream afterwards.
+    // event), so it does not wait for work queued on the caller's stream (e.g. the previous
+    // step's convolutions); the host reads its counts only when the coarse grid is first used.
+    // Buffers are allocated for the build stream and handed to the caller's stream.
     auto main = at::cuda::getCurrentCUDAStream(dev.index());
     auto side = build_stream(dev.index());
     if (g->ready) g->ready->block(side);
@@ -301,53 +336,72 @@ GridPtr build_coarse_by_leaves(const GridPtr &g, const Vec3 &f, const int32_t lo
         e.record(main);
         e.block(side);
     }
-    Tensor out_ijk, leaf_ids, meta;
-    int64_t *h = pinned_meta(dev.index(), (size_t)(B + 4));
+    auto pb = std::make_unique<GridImpl::PendingBuild>();
+    pb->meta_host = torch::empty({B + 4}, torch::dtype(torch::kInt64).pinned_memory(true));
     {
         c10::cuda::CUDAStreamGuard sg(side);
-        out_ijk = torch::empty({std::max<int64_t>(g->N, 1), 3}, i32);
-        leaf_ids = torch::empty({std::max<int64_t>(g->N, 1)}, i32);
-        meta = torch::zeros({B + 4}, torch::dtype(torch::kInt64).device(dev));
+        pb->out_ijk = torch::empty({std::max<int64_t>(g->N, 1), 3}, i32);
+        pb->leaf_ids = torch::empty({std::max<int64_t>(g->N, 1)}, i32);
+        pb->meta = torch::zeros({B + 4}, torch::dtype(torch::kInt64).device(dev));
         size_t wsb = 0;
         check_status(fvgb_coarse_grid_workspace(g->L, &wsb), "coarse grid (workspace)");
         Tensor ws = workspace(wsb, dev);
         FvgbGrid fv = g->view();
         cudaStream_t cs = side.stream();
-        check_status(fvgb_coarse_grid_build(&fv, f.v, lo, hi, out_ijk.data_ptr<int32_t>(), meta.data_ptr<int64_t>(),
-                                            leaf_ids.data_ptr<int32_t>(), ws.data_ptr(), ws.numel(), cs),
+        check_status(fvgb_coarse_grid_build(&fv, f.v, lo, hi, pb->out_ijk.data_ptr<int32_t>(),
+                                            pb->meta.data_ptr<int64_t>(), pb->leaf_ids.data_ptr<int32_t>(),
+                                            ws.data_ptr(), ws.numel(), cs),
                      "coarse grid");
-        TORCH_CHECK(cudaMemcpyAsync(h, meta.data_ptr<int64_t>(), (B + 4) * sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                    cs) == cudaSuccess &&
-                        cudaStreamSynchronize(cs) == cudaSuccess,
-                    "coarse grid: reading the counts failed");
+        TORCH_CHECK(cudaMemcpyAsync(pb->meta_host.data_ptr<int64_t>(), pb->meta.data_ptr<int64_t>(),
+                                    (B + 4) * sizeof(int64_t), cudaMemcpyDeviceToHost, cs) == cudaSuccess,
+                    "coarse grid: copying the counts failed");
+        pb->counted.record(side);
     }
-    // the build stream is idle again; its buffers live on in the caller's stream
-    out_ijk.record_stream(main);
-    leaf_ids.record_stream(main);
-    meta.record_stream(main);
-    auto s = cur_stream();
-    for (int a = 0; a < 3; ++a) {
-        c->box_lo[a] = lo[a];
-        c->box_hi[a] = hi[a];
-    }
-    c->joffsets_host = torch::from_blob(h, {B + 1}, torch::kInt64).clone();
-    c->joffsets = meta.narrow(0, 0, B + 1);
-    c->N = h[B + 2];
-    c->ijk = out_ijk.narrow(0, 0, c->N);
-    c->L = h[B + 1];
-    c->cap = next_pow2(2 * c->L);
-    c->leaves = torch::empty({std::max<int64_t>(c->L, 1) * (int64_t)sizeof(FvgbLeaf)},
-                             torch::dtype(torch::kUInt8).device(dev));
-    c->hash = torch::empty({c->cap}, i32);
-    FvgbGrid v = c->view();
-    check_status(fvgb_grid_index_build(&v, leaf_ids.data_ptr<int32_t>(), s), "coarse grid (index)");
-    c->ready = std::make_shared<at::cuda::CUDAEvent>();
-    c->ready->record(main);
+    // the buffers live on in the caller's stream
+    pb->out_ijk.record_stream(main);
+    pb->leaf_ids.record_stream(main);
+    pb->meta.record_stream(main);
+    c->joffsets = pb->meta.narrow(0, 0, B + 1);  // the device, for guards; values after resolve()
+    c->N = -1;
+    c->L = -1;
+    c->pending = std::move(pb);
+    c->is_pending.store(true, std::memory_order_release);
     return c;
+}
+
+void GridImpl::resolve() const {
+    if (!is_pending.load(std::memory_order_acquire)) return;
+    auto *self = const_cast<GridImpl *>(this);  // grids are created non-const; resolving fills them in
+    std::lock_guard<std::mutex> lock(self->resolve_mu);
+    if (!self->is_pending.load(std::memory_order_acquire)) return;
+    PendingBuild &P = *self->pending;
+    const auto dev = P.meta.device();
+    c10::cuda::CUDAGuard guard(dev);
+    P.counted.synchronize();  // the host waits for the coarse build alone
+    const int64_t *h = P.meta_host.data_ptr<int64_t>();
+    self->joffsets_host = P.meta_host.narrow(0, 0, B + 1).clone();
+    self->joffsets = P.meta.narrow(0, 0, B + 1);
+    self->N = h[B + 2];
+    self->L = h[B + 1];
+    self->ijk = P.out_ijk.narrow(0, 0, self->N);
+    self->cap = next_pow2(2 * self->L);
+    auto main = at::cuda::getCurrentCUDAStream(dev.index());
+    P.counted.block(main);  // the index build follows the coarse build on the device
+    auto i32 = torch::dtype(torch::kInt32).device(dev);
+    self->leaves = torch::empty({std::max<int64_t>(self->L, 1) * (int64_t)sizeof(FvgbLeaf)},
+                                torch::dtype(torch::kUInt8).device(dev));
+    self->hash = torch::empty({self->cap}, i32);
+    FvgbGrid v = self->view_unchecked();
+    check_status(fvgb_grid_index_build(&v, P.leaf_ids.data_ptr<int32_t>(), main.stream()), "coarse grid (index)");
+    self->ready = std::make_shared<at::cuda::CUDAEvent>();
+    self->ready->record(main);
+    self->pending.reset();
+    self->is_pending.store(false, std::memory_order_release);
 }
 
 // conv_grid: output voxel set of a (strided) convolution (BuildGridForConv.cu:181-255).
 GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, const std::vector<int64_t> &st_in) {
+    R(g);
     c10::cuda::CUDAGuard guard(g->device());
     Vec3 ks = to_vec3(ks_in, "kernel_size"), st = to_vec3(st_in, "stride");
     for (int a = 0; a < 3; ++a) {
@@ -420,6 +474,7 @@ GridPtr grid_conv_grid(const GridPtr &g, const std::vector<int64_t> &ks_in, cons
 }
 
 Tensor grid_ijk_to_index(const GridPtr &g, const Tensor &ijk_in, const Tensor &joff_in, bool cumulative) {
+    R(g);
     c10::cuda::CUDAGuard guard(g->device());
     TORCH_CHECK_VALUE(ijk_in.dim() == 2 && ijk_in.size(1) == 3, "ijk must have shape (N, 3)");
     Tensor q = ijk_in.to(g->device(), torch::kInt32).contiguous();
@@ -434,6 +489,7 @@ Tensor grid_ijk_to_index(const GridPtr &g, const Tensor &ijk_in, const Tensor &j
 }
 
 Tensor grid_jidx(const GridPtr &g) {
+    R(g);
     if (!g->jidx_cache.defined()) {
         Tensor counts = (g->joffsets_host.narrow(0, 1, g->B) - g->joffsets_host.narrow(0, 0, g->B));
         g->jidx_cache = torch::repeat_interleave(torch::arange(g->B, torch::kInt32), counts).to(g->device());
@@ -469,8 +525,16 @@ struct PackInfo {
 };
 using PackPtr = std::shared_ptr<PackInfo>;
 
+void resolve_pack(const PackPtr &p) {
+    if (!p) return;
+    R(p->src);
+    R(p->tgt);
+}
+
 PackPtr make_pack(const std::vector<int64_t> &ks_in, const std::vector<int64_t> &st_in, const GridPtr &src,
                   const std::optional<GridPtr> &tgt) {
+    R(src);
+    if (tgt) R(*tgt);
     auto p = std::make_shared<PackInfo>();
     p->ks = to_vec3(ks_in, "kernel_size");
     p->st = to_vec3(st_in, "stride");
@@ -511,6 +575,7 @@ Tensor build_kmap(const GridPtr &src, const GridPtr &tgt, const Vec3 &ks, const 
 }
 
 const Tensor &pack_kmap(PackPtr p) {
+    resolve_pack(p);
     if (!p->out_in_map) {
         Tensor tm;
         p->out_in_map = build_kmap(p->src, p->tgt, p->ks, p->st, p->K, &tm);
@@ -520,6 +585,7 @@ const Tensor &pack_kmap(PackPtr p) {
 }
 
 const Tensor &pack_kmap_t(PackPtr p) {
+    resolve_pack(p);
     if (!p->out_in_map_bwd) {
         const Tensor &m = pack_kmap(p);
         const int64_t npad = (p->src->N + 127) / 128 * 128;
@@ -544,6 +610,7 @@ Tensor tile_masks_of(const Tensor &map, int64_t n_rows, int32_t K) {
 
 // Per-tile occupancy of the forward map (transposed=false) or of the transposed map.
 std::optional<Tensor> pack_tile_mask(PackPtr p, bool transposed) {
+    resolve_pack(p);
     if (p->K > 32) return std::nullopt;
     if (!transposed) {
         if (!p->tile_mask) p->tile_mask = tile_masks_of(pack_kmap(p), p->tgt->N, p->K);
@@ -575,6 +642,7 @@ struct RowOrder {
 };
 
 std::optional<RowOrder> pack_row_order(PackPtr p, bool transposed) {
+    resolve_pack(p);
     if (p->K < 4 || p->K > 32) return std::nullopt;
     const int d = transposed ? 1 : 0;
     if (!p->order_rows[d]) {
@@ -626,6 +694,7 @@ std::optional<Tensor> pack_plan_if_reused(PackPtr p, bool transposed, int32_t ro
 // (transposed=false) or of the transposed map, for feature rows of row_bytes bytes; built once
 // per pack and row size.  nullopt where the planned kernel does not take the shape.
 std::optional<Tensor> pack_plan(PackPtr p, bool transposed, int32_t row_bytes) {
+    resolve_pack(p);
     if (p->K > 32) return std::nullopt;
     const auto key = std::make_pair(transposed ? 1 : 0, row_bytes);
     auto it = p->plans.find(key);
@@ -643,6 +712,7 @@ std::optional<Tensor> pack_plan(PackPtr p, bool transposed, int32_t row_bytes) {
 }
 
 void pack_build_gather_scatter(PackPtr p, bool use_me) {
+    resolve_pack(p);
     if (p->nbmap && p->nbsizes) {
         TORCH_CHECK(p->gs_use_me.value_or(use_me) == use_me, "Gather scatter is already built with different use_me value");
         return;
@@ -707,6 +777,7 @@ Tensor reduce_mask(const Tensor &sorted_mask, int64_t tile) {
 }
 
 void pack_build_implicit_gemm(PackPtr p, bool sorted, int64_t split, bool training, int64_t split_bwd, bool tf32) {
+    resolve_pack(p);
     if (p->reorder_loc && sorted)
         TORCH_CHECK(p->reorder_loc->size(0) == split, "Implicit GEMM is already built with different splitMaskNum value");
     c10::cuda::CUDAGuard guard(p->tgt->device());
@@ -974,6 +1045,7 @@ Tensor gather_wgrad(const Tensor &x, const Tensor &map, int64_t n_out, const Ten
 // relu: the output is max(conv + bias, 0), fused into the tensor-core epilogue.
 std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed,
                                  const std::optional<Tensor> &bias = std::nullopt, bool relu = false) {
+    resolve_pack(p);
     TORCH_CHECK_VALUE(x.is_contiguous(), "features must be contiguous");
     TORCH_CHECK_TYPE(x.is_floating_point(), "features must have a floating point type");
     TORCH_CHECK_VALUE(x.dim() == 2, "Expected features to have 2 dimensions (shape (n, nF)) but got ", x.dim(),
@@ -1034,6 +1106,7 @@ std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr
 // Returns (dx, dW) with dW in the 5-D layout of the forward weights.
 std::vector<Tensor> conv_backward(const Tensor &dy_in, const Tensor &x, const Tensor &Wkio, PackPtr p, bool transposed,
                                   bool need_dx, bool need_dw) {
+    resolve_pack(p);
     Tensor dy = dy_in.contiguous();
     const int64_t K = Wkio.size(0), cin = Wkio.size(1), cout = Wkio.size(2);
     Tensor dx, dW;
@@ -1060,6 +1133,7 @@ std::vector<Tensor> conv_backward(const Tensor &dy_in, const Tensor &x, const Te
 // Returns (y bf16, s_x, s_w).
 std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed,
                                      bool relu = false) {
+    resolve_pack(p);
     TORCH_CHECK_VALUE(x.dim() == 2 && x.is_cuda() && x.is_floating_point(), "features must be a 2-D CUDA float tensor");
     TORCH_CHECK_VALUE(weights.dim() == 5, "Expected kernels to have 5 dimensions");
     c10::cuda::CUDAGuard guard(x.device());
@@ -1128,6 +1202,7 @@ std::vector<Tensor> conv_forward_fp8(const Tensor &x, const Tensor &weights, Pac
 // coarsened_grid(f): floor(ijk / f) per axis (GridBatch::coarsened_grid, BuildCoarseGridFromFine.cu:22-82),
 // the coarse path of conv_grid with kernel == stride == f.
 GridPtr grid_coarsened(const GridPtr &g, const std::vector<int64_t> &f) {
+    R(g);
     Vec3 v = to_vec3(f, "coarsening_factor");
     for (int a = 0; a < 3; ++a) TORCH_CHECK_VALUE(v.v[a] > 0, "coarsening_factor must be positive");
     std::vector<int64_t> ff = {v.v[0], v.v[1], v.v[2]};
@@ -1142,6 +1217,7 @@ GridPtr grid_coarsened(const GridPtr &g, const std::vector<int64_t> &f) {
 // subdivided_grid(f, mask): every (masked) voxel c gives c*f + (i,j,k) (GridBatch::subdivided_grid,
 // BuildFineGridFromCoarse.cu:66-226).
 GridPtr grid_subdivided(const GridPtr &g, const std::vector<int64_t> &f, const std::optional<Tensor> &mask) {
+    R(g);
     c10::cuda::CUDAGuard guard(g->device());
     Vec3 v = to_vec3(f, "subdiv_factor");
     for (int a = 0; a < 3; ++a) TORCH_CHECK_VALUE(v.v[a] > 0, "subdiv_factor must be positive");
@@ -1190,6 +1266,8 @@ Tensor flat2d(const Tensor &t) { return t.reshape({t.size(0), -1}).contiguous();
 // y [coarse N, C] = max / average pooling of x [fine N, *] (mode FVGB_POOL_MAX / FVGB_POOL_AVG)
 Tensor pool_forward(int32_t mode, const GridPtr &fine, const GridPtr &coarse, const std::vector<int64_t> &pool,
                     const std::vector<int64_t> &stride, const Tensor &x) {
+    R(fine);
+    R(coarse);
     c10::cuda::CUDAGuard guard(fine->device());
     TORCH_CHECK_VALUE(x.dim() > 1, "fine_data must have more than one dimension. i.e. have shape (num_voxels, *)");
     TORCH_CHECK_VALUE(x.size(0) == fine->N, "fine_data must have the same number of voxels as fine_grid");
@@ -1216,6 +1294,8 @@ Tensor pool_forward(int32_t mode, const GridPtr &fine, const GridPtr &coarse, co
 
 Tensor pool_backward(int32_t mode, const GridPtr &fine, const GridPtr &coarse, const std::vector<int64_t> &pool,
                      const std::vector<int64_t> &stride, const Tensor &x, const Tensor &dy) {
+    R(fine);
+    R(coarse);
     c10::cuda::CUDAGuard guard(fine->device());
     Vec3 p = to_vec3(pool, "pool_factor"), st = to_vec3(stride, "stride");
     for (int a = 0; a < 3; ++a)
@@ -1243,6 +1323,7 @@ Tensor pool_backward(int32_t mode, const GridPtr &fine, const GridPtr &coarse, c
 // Stride-1 3^3 convolution over the grid without a kernel map: y = sum_k x[v + d_k] W[k] for
 // W [27, Cin, Cout] (mirror: the data gradient, W[26-k]^T with W in the forward's layout).
 Tensor halo_conv(const GridPtr &g, const Tensor &x, const Tensor &w, bool mirror) {
+    R(g);
     c10::cuda::CUDAGuard guard(g->device());
     TORCH_CHECK_VALUE(x.dim() == 2 && x.size(0) == g->N, "features must have shape (num_voxels, channels)");
     TORCH_CHECK_VALUE(w.dim() == 3 && w.size(0) == 27, "halo weights must have shape (27, in, out)");
@@ -1264,6 +1345,7 @@ Tensor halo_conv(const GridPtr &g, const Tensor &x, const Tensor &w, bool mirror
 
 // dW [27, Cin, Cout] = sum_v x[v + d_k]^T dy[v] (fixed-order FP64 sum of per-chunk partials)
 Tensor halo_wgrad(const GridPtr &g, const Tensor &x, const Tensor &dy) {
+    R(g);
     c10::cuda::CUDAGuard guard(g->device());
     TORCH_CHECK_VALUE(x.dim() == 2 && dy.dim() == 2 && x.size(0) == g->N && dy.size(0) == g->N,
                       "features and gradients must have shape (num_voxels, channels)");
@@ -1284,6 +1366,8 @@ Tensor halo_wgrad(const GridPtr &g, const Tensor &x, const Tensor &dy) {
 
 // y [fine N, *] = nearest upsampling of x [coarse N, *]
 Tensor upsample_forward(const GridPtr &coarse, const GridPtr &fine, const std::vector<int64_t> &factor, const Tensor &x) {
+    R(fine);
+    R(coarse);
     c10::cuda::CUDAGuard guard(fine->device());
     TORCH_CHECK_VALUE(x.dim() > 1 && x.size(0) == coarse->N, "data must have shape (num_voxels, *) of the coarse grid");
     Vec3 f = to_vec3(factor, "subdiv_factor");
@@ -1303,6 +1387,8 @@ Tensor upsample_forward(const GridPtr &coarse, const GridPtr &fine, const std::v
 
 Tensor upsample_backward(const GridPtr &coarse, const GridPtr &fine, const std::vector<int64_t> &factor, const Tensor &dy,
                          const Tensor &x) {
+    R(fine);
+    R(coarse);
     c10::cuda::CUDAGuard guard(fine->device());
     Vec3 f = to_vec3(factor, "subdiv_factor");
     Tensor df = flat2d(dy.to(x.scalar_type()));
@@ -1336,15 +1422,15 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
         .def("coarsened_grid", &grid_coarsened, py::call_guard<py::gil_scoped_release>())
         .def("subdivided_grid", &grid_subdivided, py::arg("subdiv_factor"), py::arg("mask") = py::none())
         .def_property_readonly("grid_count", [](const GridImpl &g) { return g.B; })
-        .def_property_readonly("total_voxels", [](const GridImpl &g) { return g.N; })
-        .def_property_readonly("total_leaf_nodes", [](const GridImpl &g) { return g.L; })
-        .def_property_readonly("ijk", [](const GridImpl &g) { return g.ijk; })
-        .def_property_readonly("joffsets", [](const GridImpl &g) { return g.joffsets; })
-        .def_property_readonly("joffsets_host", [](const GridImpl &g) { return g.joffsets_host; })
+        .def_property_readonly("total_voxels", [](const GridImpl &g) { g.resolve(); return g.N; })
+        .def_property_readonly("total_leaf_nodes", [](const GridImpl &g) { g.resolve(); return g.L; })
+        .def_property_readonly("ijk", [](const GridImpl &g) { g.resolve(); return g.ijk; })
+        .def_property_readonly("joffsets", [](const GridImpl &g) { g.resolve(); return g.joffsets; })
+        .def_property_readonly("joffsets_host", [](const GridImpl &g) { g.resolve(); return g.joffsets_host; })
         .def_property_readonly("voxel_sizes", [](const GridImpl &g) { return g.voxel_sizes; })
         .def_property_readonly("origins", [](const GridImpl &g) { return g.origins; })
-        .def_property_readonly("leaves", [](const GridImpl &g) { return g.leaves; })
-        .def_property_readonly("hash", [](const GridImpl &g) { return g.hash; })
+        .def_property_readonly("leaves", [](const GridImpl &g) { g.resolve(); return g.leaves; })
+        .def_property_readonly("hash", [](const GridImpl &g) { g.resolve(); return g.hash; })
         .def_property_readonly("device", [](const GridImpl &g) { return g.device(); })
         .def("jidx", [](GridPtr g) { return grid_jidx(g); })
         .def("ijk_to_index", &grid_ijk_to_index);
