@@ -871,11 +871,14 @@ def leg_serve(fvdb, dev, args) -> dict:
         ex = GPUExecutor(mdl, dev, slots=slots)
         srv_args = dict(hbm_budget=48 << 30, max_batch_voxels=4_000_000, slots=slots, max_batch_requests=per_batch)
         servers[name] = (ex, srv_args)
-        # warm-up: the smallest and the largest request of the pool alone (first-call and
-        # allocator-growth costs stay out of the measured latencies)
+        # warm-up: the smallest and the largest request of the pool alone, then every pool grid
+        # once at a high rate (first-call costs and the allocator's growth to batch sizes stay out
+        # of the measured latencies)
         for j in (min(range(len(pool)), key=lambda i: pool[i][0].shape[0]),
                   max(range(len(pool)), key=lambda i: pool[i][0].shape[0])):
             ContinuousBatcher(ex, **srv_args).serve([Request(rid=-1, ijk=pool[j][0], features=pool[j][1], arrival=0.0)])
+        ContinuousBatcher(ex, **srv_args).serve([Request(rid=-2 - j, ijk=pool[j][0], features=pool[j][1],
+                                                         arrival=0.001 * j) for j in range(len(pool))])
     sample_done = {}
     for ri, rate in enumerate(rates):
         r2 = np.random.default_rng(1000 + ri)
