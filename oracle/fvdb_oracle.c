@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the sparse-convolution index path.  TEST INFRASTRUCTURE ONLY:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this
- * library, and only as the checker.  The product never links or calls it.
+ * library, and only to compare results against.  The product never links or calls it.
  *
  * It restates, in plain C, the integer algorithms of fVDB 0.2.1 (reference paths
  * relative to the fvdb-core source tree):

@@ -1,7 +1,8 @@
 """CPU oracle of the sparse-convolution path -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this module,
-and only as the checker / the timed CPU baseline.  The fvdb_gb300 package never imports it.
+and only to compare results against / as the timed CPU baseline.  The fvdb_gb300 package never
+imports it.
 
 Contents (reference paths relative to the fvdb-core tree):
   grid_from_ijk        voxel index order of BuildGridFromIjk.cu:26-83 (fvdb_oracle.c)
