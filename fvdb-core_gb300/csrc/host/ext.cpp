@@ -909,7 +909,7 @@ void derived_put(const Tensor &src, int tag, const Tensor &value) {
 Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tensor &Wkio, bool transpose_w,
                    const std::optional<Tensor> &tile_mask = std::nullopt,
                    const std::optional<Tensor> &bias = std::nullopt, PackPtr pack = nullptr, bool map_t = false,
-                   bool relu = false) {
+                   bool relu = false, const std::optional<Tensor> &out_scale = std::nullopt) {
     c10::cuda::CUDAGuard guard(x.device());
     const int64_t K = map.size(1);
     const int64_t cin = transpose_w ? Wkio.size(2) : Wkio.size(1);
@@ -937,8 +937,10 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
             if (Wkio.scalar_type() == torch::kBFloat16) derived_put(Wkio, tag, packed);
         }
         const uint32_t *tm = tile_mask ? reinterpret_cast<const uint32_t *>(tile_mask->data_ptr<int32_t>()) : nullptr;
-        Tensor b32;
+        Tensor b32, s32;
         if (bias) b32 = bias->to(torch::kFloat32).contiguous();
+        if (out_scale) s32 = out_scale->to(torch::kFloat32).contiguous();
+        const float *sp = out_scale ? s32.data_ptr<float>() : nullptr;
         // a map used again runs over its row order (measured faster than a tile plan: C2 layer 1,
         // 32->64: 0.30 ms ordered, 0.32 ms planned, 0.365 ms in index order); the tile plan serves
         // maps that have no row order (K < 4 or K > 32)
@@ -951,7 +953,7 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
                                                order->map.data_ptr<int32_t>(), n_out, (int32_t)K,
                                                order->rows.data_ptr<int32_t>(),
                                                reinterpret_cast<const uint32_t *>(order->mask.data_ptr<int32_t>()),
-                                               packed.data_ptr(), (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
+                                               packed.data_ptr(), (int32_t)cout, y.data_ptr(), y.stride(0), sp,
                                                bias ? b32.data_ptr<float>() : nullptr, relu ? 1 : 0,
                                                device_error_flag(x.device()).data_ptr<int32_t>(), s),
                          "sparse conv forward (tensor cores)");
@@ -960,7 +962,7 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
         if (plan) {
             check_status(fvgb_conv_fwd_tc_planned(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
                                                   plan->data_ptr(), n_out, (int32_t)K, packed.data_ptr(),
-                                                  (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
+                                                  (int32_t)cout, y.data_ptr(), y.stride(0), sp,
                                                   bias ? b32.data_ptr<float>() : nullptr, relu ? 1 : 0,
                                                   device_error_flag(x.device()).data_ptr<int32_t>(), s),
                          "sparse conv forward (tensor cores)");
@@ -968,7 +970,7 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
         }
         check_status(fvgb_conv_fwd_tc_epilogue(FVGB_BF16, x.data_ptr(), x.size(0), (int32_t)cin, x.stride(0),
                                                map.data_ptr<int32_t>(), n_out, (int32_t)K, tm, packed.data_ptr(),
-                                               (int32_t)cout, y.data_ptr(), y.stride(0), nullptr,
+                                               (int32_t)cout, y.data_ptr(), y.stride(0), sp,
                                                bias ? b32.data_ptr<float>() : nullptr, relu ? 1 : 0,
                                                device_error_flag(x.device()).data_ptr<int32_t>(), s),
                      "sparse conv forward (tensor cores)");
@@ -998,6 +1000,7 @@ Tensor gather_gemm(const Tensor &x, const Tensor &map, int64_t n_out, const Tens
                      "sparse conv forward");
         y.copy_(yf);
     }
+    if (out_scale) y.mul_(out_scale->to(y.scalar_type()));
     if (bias) y.add_(bias->to(y.scalar_type()));
     if (relu) y.relu_();
     return y;
@@ -1042,9 +1045,12 @@ Tensor gather_wgrad(const Tensor &x, const Tensor &map, int64_t n_out, const Ten
 // ------------------------------------------------------------------------------------------
 // Forward / backward of one sparse convolution, called by the Python autograd Function.
 // Checks and permutes follow SparseConvolutionKernelMap.cpp:18-191.
-// relu: the output is max(conv + bias, 0), fused into the tensor-core epilogue.
+// relu: the output is max(conv + bias, 0), fused into the tensor-core epilogue; out_scale
+// (optional, [Cout]): the output is conv * out_scale + bias (an inference-mode batch norm folded
+// into the layer), also in the epilogue.
 std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr p, bool transposed,
-                                 const std::optional<Tensor> &bias = std::nullopt, bool relu = false) {
+                                 const std::optional<Tensor> &bias = std::nullopt, bool relu = false,
+                                 const std::optional<Tensor> &out_scale = std::nullopt) {
     resolve_pack(p);
     TORCH_CHECK_VALUE(x.is_contiguous(), "features must be contiguous");
     TORCH_CHECK_TYPE(x.is_floating_point(), "features must have a floating point type");
@@ -1093,12 +1099,19 @@ std::vector<Tensor> conv_forward(const Tensor &x, const Tensor &weights, PackPtr
         TORCH_CHECK_VALUE(bias->dim() == 1 && bias->size(0) == cout, "bias must have shape (", cout, ",)");
         TORCH_CHECK_VALUE(bias->device() == x.device(), "bias must be on the features' device");
     }
+    if (out_scale) {
+        TORCH_CHECK_VALUE(out_scale->dim() == 1 && out_scale->size(0) == cout, "out_scale must have shape (", cout,
+                          ",)");
+        TORCH_CHECK_VALUE(out_scale->device() == x.device(), "out_scale must be on the features' device");
+    }
     Tensor y;
     if (!transposed)
-        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false), bias, p, false, relu)
+        y = n_tgt > 0 ? gather_gemm(x, pack_kmap(p), n_tgt, Wkio, false, pack_tile_mask(p, false), bias, p, false, relu,
+                                    out_scale)
                       : torch::empty({0, cout}, x.options());
     else
-        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true), bias, p, true, relu)
+        y = n_src > 0 ? gather_gemm(x, pack_kmap_t(p), n_src, Wkio, false, pack_tile_mask(p, true), bias, p, true, relu,
+                                    out_scale)
                       : torch::empty({0, cout}, x.options());
     return {y, Wkio};
 }
@@ -1471,7 +1484,7 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
     // so host threads of concurrent serving slots do not serialise on it
     m.def("conv_forward", &conv_forward, py::arg("features"), py::arg("weights"), py::arg("pack"),
           py::arg("transposed"), py::arg("bias") = py::none(), py::arg("relu") = false,
-          py::call_guard<py::gil_scoped_release>());
+          py::arg("out_scale") = py::none(), py::call_guard<py::gil_scoped_release>());
     m.def("conv_forward_fp8", &conv_forward_fp8, py::arg("features"), py::arg("weights"), py::arg("pack"),
           py::arg("transposed"), py::arg("relu") = false, py::call_guard<py::gil_scoped_release>());
     m.def("check_device_errors", [](const torch::Device &d) { check_device_errors(d); },

@@ -18,9 +18,10 @@ from . import _lib
 class SparseConvFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, features: torch.Tensor, weights: torch.Tensor, pack_impl, transposed: bool, bias=None,
-                relu: bool = False):
+                relu: bool = False, scale=None):
         C = _lib.load()
-        y, wkio = C.conv_forward(features, weights, pack_impl, transposed, bias, relu)
+        y, wkio = C.conv_forward(features, weights, pack_impl, transposed, bias, relu, scale)
+        ctx.scaled = scale is not None
         if relu:
             ctx.save_for_backward(features, wkio, y)
         else:
@@ -37,7 +38,9 @@ class SparseConvFunction(torch.autograd.Function):
         features, wkio = ctx.saved_tensors[:2]
         need_dx, need_dw, need_db = ctx.needs_input_grad[0], ctx.needs_input_grad[1], ctx.needs_input_grad[4]
         if grad_out is None or not (need_dx or need_dw or need_db):
-            return None, None, None, None, None, None
+            return None, None, None, None, None, None, None
+        if ctx.scaled:
+            raise RuntimeError("a convolution with a folded batch norm (out_scale) is inference-only")
         if ctx.relu:
             # fused ReLU: the gradient passes where the output is positive (torch.relu's rule)
             grad_out = grad_out * (ctx.saved_tensors[2] > 0)
@@ -49,12 +52,13 @@ class SparseConvFunction(torch.autograd.Function):
         if need_db:
             acc = torch.promote_types(grad_out.dtype, torch.float32)
             db = grad_out.sum(0, dtype=acc).to(ctx.bias_dtype)
-        return (dx if need_dx else None), (dw if need_dw else None), None, None, db, None
+        return (dx if need_dx else None), (dw if need_dw else None), None, None, db, None, None
 
 
 def sparse_conv(features: torch.Tensor, weights: torch.Tensor, pack_impl, transposed: bool, bias=None,
-                relu: bool = False) -> torch.Tensor:
+                relu: bool = False, scale=None) -> torch.Tensor:
     """One sparse convolution with autograd; `bias` ([C_out], optional) is added, and with `relu`
     the output clamped at zero, in the contraction's epilogue on the tensor-core path (one pass
-    over the output instead of two or three)."""
-    return SparseConvFunction.apply(features, weights, pack_impl, transposed, bias, relu)
+    over the output instead of two or three).  `scale` ([C_out], optional, inference only)
+    multiplies the contraction before the bias: an eval-mode batch norm folded into the layer."""
+    return SparseConvFunction.apply(features, weights, pack_impl, transposed, bias, relu, scale)

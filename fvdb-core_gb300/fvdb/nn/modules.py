@@ -79,7 +79,8 @@ class SparseConv3d(nn.Module):
         if self.bias is not None:
             self.bias.data.uniform_(-std, std)
 
-    def _dispatch_conv(self, in_feature, in_grid: GridBatch, in_kmap, out_grid, relu: bool = False):
+    def _dispatch_conv(self, in_feature, in_grid: GridBatch, in_kmap, out_grid, relu: bool = False, scale=None,
+                       shift=None):
         can_cache = self.stride == (1, 1, 1) and (out_grid is None or out_grid.is_same(in_grid))
         if in_kmap is not None and in_kmap.kernel_size == self.kernel_size and can_cache:
             kmap, out_grid = in_kmap, in_grid
@@ -94,22 +95,40 @@ class SparseConv3d(nn.Module):
             kmap.build_implicit_gemm(sorted=False, training=False)
         prec = None if self.precision == "native" else self.precision
         # the bias is added in the contraction's epilogue (the reference adds it in a second pass)
-        out_feature = kmap._conv_with_bias(in_feature, self.weight, self.bias, self.transposed, prec, relu)
+        bias = self.bias if scale is None else shift
+        out_feature = kmap._conv_with_bias(in_feature, self.weight, bias, self.transposed, prec, relu, scale)
         return out_grid, out_feature, out_kmap
 
-    def forward(self, input: VDBTensor, out_grid: Optional[GridBatch] = None, *, relu: bool = False) -> VDBTensor:
+    def _folded(self, out_affine):
+        """(scale, shift) of conv * scale + shift with a following per-channel affine map
+        (s, t) folded in: scale = s, shift = bias * s + t (FP32)."""
+        s, t = (v.detach().float() for v in out_affine)
+        return s, (t if self.bias is None else self.bias.detach().float() * s + t)
+
+    def forward(self, input: VDBTensor, out_grid: Optional[GridBatch] = None, *, relu: bool = False,
+                out_affine=None) -> VDBTensor:
         """`relu` (extension): return max(conv(input) + bias, 0), the clamp fused into the
-        contraction's epilogue (nn.Sequential passes it for a SparseConv3d followed by a ReLU)."""
+        contraction's epilogue (nn.Sequential passes it for a SparseConv3d followed by a ReLU).
+        `out_affine` (extension, inference only): a pair (s, t) of [C_out] tensors; the output is
+        (conv(input) + bias) * s + t, applied in FP32 in the epilogue with the features' dtype
+        kept (nn.Sequential passes it to fold an eval-mode BatchNorm into the convolution)."""
         in_feature, in_grid, in_kmap = input.data, input.grid, input.kmap
+        scale = shift = None
+        if out_affine is not None:
+            if torch.is_grad_enabled() and (self.weight.requires_grad or in_feature.jdata.requires_grad):
+                raise RuntimeError("out_affine (a folded batch norm) is inference-only")
+            scale, shift = self._folded(out_affine)
         if self.kernel_size == (1, 1, 1) and self.stride == (1, 1, 1):
-            out_feature = in_feature.jagged_like(in_feature.jdata.matmul(self.weight.transpose(0, 1)))
+            y = in_feature.jdata.matmul(self.weight.transpose(0, 1))
+            if scale is not None:
+                y = (y.float() * scale + shift).to(y.dtype)
+            elif self.bias is not None:
+                y = y + self.bias
+            out_feature = in_feature.jagged_like(torch.relu(y) if relu else y)
             out_grid, out_kmap = in_grid, in_kmap
-            if self.bias is not None:
-                out_feature.jdata = out_feature.jdata + self.bias
-            if relu:
-                out_feature.jdata = torch.relu(out_feature.jdata)
         else:
-            out_grid, out_feature, out_kmap = self._dispatch_conv(in_feature, in_grid, in_kmap, out_grid, relu)
+            out_grid, out_feature, out_kmap = self._dispatch_conv(in_feature, in_grid, in_kmap, out_grid, relu, scale,
+                                                                  shift)
         if out_grid is None:
             raise ValueError("Failed to compute output grid. This is a bug in the implementation.")
         return VDBTensor(out_grid, out_feature, out_kmap)
@@ -122,10 +141,65 @@ class ReLU(nn.ReLU):
         return VDBTensor(input.grid, input.data.jagged_like(super().forward(input.data.jdata)), input.kmap)
 
 
+class BatchNorm(nn.BatchNorm1d):
+    """Batch normalisation of a VDBTensor's features over all voxels of the batch (reference:
+    fvdb/nn/modules.py:435-444): torch's BatchNorm1d on the [N, C] feature matrix."""
+
+    def forward(self, input: VDBTensor) -> VDBTensor:
+        if input.data.jdata.size(1) != self.num_features:
+            raise ValueError("Input feature should have the same number of channels as BatchNorm")
+        return VDBTensor(input.grid, input.grid.jagged_like(super().forward(input.data.jdata)), input.kmap)
+
+    def folded_affine(self):
+        """(s, t), FP32 [C]: the eval-mode map x -> x * s + t this layer applies with its
+        running statistics, or None when it normalises with batch statistics."""
+        if self.training or self.running_mean is None or self.running_var is None:
+            return None
+        s = torch.rsqrt(self.running_var.detach().float() + self.eps)
+        if self.weight is not None:
+            s = s * self.weight.detach().float()
+        t = -self.running_mean.detach().float() * s
+        if self.bias is not None:
+            t = t + self.bias.detach().float()
+        return s, t
+
+
+class GroupNorm(nn.GroupNorm):
+    """Group normalisation of a VDBTensor's features, per grid of the batch (reference:
+    fvdb/nn/modules.py:408-432, which loops over the grids): each (grid, group) is normalised
+    over its voxels and the group's channels, with the biased variance and eps of
+    torch.nn.GroupNorm.  One vectorised pass over all grids: the per-(grid, group) sums are
+    segment sums keyed by the voxels' grid index, the variance is taken about the mean (two
+    passes, FP32 or wider), and empty grids contribute nothing."""
+
+    def forward(self, input: VDBTensor) -> VDBTensor:
+        x = input.data.jdata
+        n, c = x.shape[0], x.shape[1] if x.dim() == 2 else -1
+        if x.dim() != 2 or c != self.num_channels:
+            raise ValueError("Input feature should have the same number of channels as GroupNorm")
+        g, b = self.num_groups, input.grid.grid_count
+        acc = torch.float64 if x.dtype == torch.float64 else torch.float32
+        jidx = input.data.jidx.long()
+        xg = x.to(acc).reshape(n, g, c // g)
+        counts = torch.bincount(jidx, minlength=b).to(acc) * (c // g)
+        denom = counts.clamp(min=1)[:, None]
+        mean = torch.zeros(b, g, dtype=acc, device=x.device).index_add_(0, jidx, xg.sum(2)) / denom
+        d = xg - mean[jidx][:, :, None]
+        var = torch.zeros(b, g, dtype=acc, device=x.device).index_add_(0, jidx, (d * d).sum(2)) / denom
+        y = (d * torch.rsqrt(var + self.eps)[jidx][:, :, None]).reshape(n, c)
+        if self.affine:
+            y = y * self.weight.to(acc) + self.bias.to(acc)
+        return VDBTensor(input.grid, input.grid.jagged_like(y.to(x.dtype)), input.kmap)
+
+
 class Sequential(nn.Sequential):
     """nn.Sequential over VDBTensor-to-VDBTensor layers.  A SparseConv3d directly followed by a
     ReLU runs as one convolution with the ReLU fused into its epilogue: the same values (rounding
-    to the output type keeps signs) and gradients, one pass over the output instead of two."""
+    to the output type keeps signs) and gradients, one pass over the output instead of two.
+    Without autograd (inference), a SparseConv3d followed by an eval-mode BatchNorm (and
+    optionally a ReLU) runs as one convolution with the batch norm's affine map folded into the
+    epilogue's per-channel scale and shift: the values of the three layers within the rounding
+    of one output type, one pass over the output instead of three."""
 
     def forward(self, input):
         mods = list(self)
@@ -133,6 +207,15 @@ class Sequential(nn.Sequential):
         while i < len(mods):
             m = mods[i]
             nxt = mods[i + 1] if i + 1 < len(mods) else None
+            if (isinstance(m, SparseConv3d) and type(nxt) is BatchNorm and not torch.is_grad_enabled()
+                    and m.precision == "native"):
+                aff = nxt.folded_affine()
+                if aff is not None and aff[0].device == m.weight.device:
+                    after = mods[i + 2] if i + 2 < len(mods) else None
+                    relu = type(after) is ReLU
+                    input = m(input, relu=relu, out_affine=aff)
+                    i += 3 if relu else 2
+                    continue
             if isinstance(m, SparseConv3d) and type(nxt) is ReLU and not nxt.inplace:
                 input = m(input, relu=True)
                 i += 2

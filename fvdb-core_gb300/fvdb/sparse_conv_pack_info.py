@@ -51,12 +51,18 @@ def _vec(v) -> list[int]:
 
 
 def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, precision: str | None,
-           bias: torch.Tensor | None = None, relu: bool = False) -> torch.Tensor:
+           bias: torch.Tensor | None = None, relu: bool = False, scale: torch.Tensor | None = None) -> torch.Tensor:
     """One convolution in the requested arithmetic.  The result has the dtype that the
     reference's `conv(x) + bias` has (torch type promotion of the contraction's output and the
     bias): the bias is fused into the contraction's epilogue when that dtype is the output's
     own, and added afterwards (promoting) otherwise.  `relu` applies max(., 0) last, fused into
-    the epilogue with the bias."""
+    the epilogue with the bias.  `scale` (inference only) multiplies the contraction before the
+    bias: the bias is then an FP32 shift and the output keeps the features' dtype."""
+    if scale is not None and precision == "fp8":
+        # the FP8 epilogue's scale dequantises: a folded batch norm is applied after it
+        y = _apply(data, weights, impl, transposed, precision)
+        y = y * scale.to(y.dtype) + (bias.to(y.dtype) if bias is not None else 0)
+        return torch.relu(y) if relu else y
     if precision in (None, "native"):
         x, w = data, weights
     elif precision == "bf16":
@@ -74,10 +80,12 @@ def _apply(data: torch.Tensor, weights: torch.Tensor, impl, transposed: bool, pr
         return y
     else:
         raise ValueError(f"precision must be one of None, 'native', 'bf16', 'fp8' (got {precision!r})")
-    if bias is not None and torch.result_type(x, bias) != x.dtype:
+    if bias is not None and scale is None and torch.result_type(x, bias) != x.dtype:
         y = sparse_conv(x, w, impl, transposed, None) + bias
         return torch.relu(y) if relu else y
-    return sparse_conv(x, w, impl, transposed, bias, relu)
+    # with a folded batch norm (scale) the output keeps the features' dtype, as the batch norm's
+    # output does; scale and shift are applied in FP32 in the epilogue
+    return sparse_conv(x, w, impl, transposed, bias, relu, scale)
 
 
 class SparseConvPackInfo:
@@ -174,14 +182,16 @@ class SparseConvPackInfo:
         return JaggedTensor.from_data_and_offsets(out, self._impl.source_grid.joffsets)
 
     def _conv_with_bias(self, input, weights: torch.Tensor, bias: torch.Tensor | None, transposed: bool,
-                        precision: str | None = None, relu: bool = False) -> JaggedTensor:
-        """sparse_conv_3d / sparse_transpose_conv_3d plus a per-output-channel bias (and, with
-        `relu`, max(., 0)) applied in the contraction's epilogue (used by nn.SparseConv3d and
-        nn.Sequential's conv -> ReLU fusion)."""
+                        precision: str | None = None, relu: bool = False,
+                        scale: torch.Tensor | None = None) -> JaggedTensor:
+        """sparse_conv_3d / sparse_transpose_conv_3d times a per-output-channel scale (optional,
+        inference only), plus a per-output-channel bias (and, with `relu`, max(., 0)), applied in
+        the contraction's epilogue (used by nn.SparseConv3d and nn.Sequential's conv -> ReLU and
+        conv -> BatchNorm (eval) -> ReLU fusions)."""
         src, tgt = self._impl.source_grid, self._impl.target_grid
         inp, out = (tgt, src) if transposed else (src, tgt)
         data = self._features(input, inp.grid_count, inp.total_voxels)
-        y = _apply(data, weights, self._impl, transposed, precision, bias, relu)
+        y = _apply(data, weights, self._impl, transposed, precision, bias, relu, scale)
         return JaggedTensor.from_data_and_offsets(y, out.joffsets)
 
     # ---------------------------------------------------------------- devices -----------

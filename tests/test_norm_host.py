@@ -1,0 +1,38 @@
+"""Host-side algebra of the batch-norm folding: BatchNorm.folded_affine's (s, t) reproduce the
+eval-mode BatchNorm1d map x -> x * s + t, with and without the affine parameters, and a
+training-mode layer (batch statistics) folds to nothing."""
+
+import pytest
+import torch
+
+
+@pytest.mark.parametrize("affine", [True, False])
+def test_folded_affine_matches_eval_batch_norm(affine):
+    import fvdb.nn as fvnn
+
+    g = torch.Generator().manual_seed(2)
+    bn = fvnn.BatchNorm(12, affine=affine, eps=1e-3).eval()
+    with torch.no_grad():
+        bn.running_mean.copy_(torch.randn(12, generator=g))
+        bn.running_var.copy_(torch.rand(12, generator=g) + 0.1)
+        if affine:
+            bn.weight.copy_(torch.randn(12, generator=g))
+            bn.bias.copy_(torch.randn(12, generator=g))
+    x = torch.randn(50, 12, generator=g)
+    s, t = bn.folded_affine()
+    ref = torch.nn.BatchNorm1d.forward(bn, x)
+    assert torch.allclose(x * s + t, ref, rtol=1e-5, atol=1e-6)
+    bn.train()
+    assert bn.folded_affine() is None
+
+
+def test_conv_folds_bias_into_shift():
+    import fvdb.nn as fvnn
+
+    conv = fvnn.SparseConv3d(4, 6, 3, bias=True)
+    s, t = torch.rand(6) + 0.5, torch.randn(6)
+    scale, shift = conv._folded((s, t))
+    assert torch.equal(scale, s)
+    assert torch.allclose(shift, conv.bias.detach() * s + t)
+    conv_nb = fvnn.SparseConv3d(4, 6, 3, bias=False)
+    assert torch.equal(conv_nb._folded((s, t))[1], t)
