@@ -388,6 +388,33 @@ class GridBatch:
         idx = self._impl.ijk_to_index(ijk.jdata, ijk.joffsets, bool(cumulative))
         return ijk.jagged_like(idx)
 
+    def inject_from(self, src_grid: "GridBatch", src: JaggedTensor, dst: JaggedTensor | None = None,
+                    default_value: float | int | bool = 0) -> JaggedTensor:
+        """Copy per-voxel data of `src_grid` onto the voxels of this grid that `src_grid` also holds
+        (index space, grid by grid; reference: fvdb/grid_batch.py:748-789).  `dst` (optional) is
+        modified in place; without it the result starts filled with `default_value`.  One
+        leaf-hash probe per voxel of this grid (ijk_to_index), then one gather."""
+        if not isinstance(src_grid, GridBatch):
+            raise TypeError("src_grid must be a GridBatch")
+        if src_grid.grid_count != self.grid_count:
+            raise ValueError("src_grid must have the same number of grids as this grid")
+        if isinstance(src, torch.Tensor):
+            src = src_grid.jagged_like(src)
+        if src.jdata.shape[0] != src_grid.total_voxels:
+            raise ValueError("src must have one row per voxel of src_grid")
+        if dst is None:
+            dst = self.jagged_like(torch.full([self.total_voxels] + list(src.eshape), default_value,
+                                              dtype=src.dtype, device=src.device))
+        elif isinstance(dst, torch.Tensor):
+            dst = self.jagged_like(dst)
+        if list(dst.eshape) != list(src.eshape):
+            raise ValueError(f"src and dst must have the same element shape, but got src: {src.eshape}, "
+                             f"dst: {dst.eshape}")
+        idx = src_grid.ijk_to_index(self.ijk, cumulative=True).jdata.long()
+        hit = torch.nonzero(idx >= 0).squeeze(1)
+        dst.jdata[hit] = src.jdata[idx[hit]].to(dst.dtype)
+        return dst
+
     def to(self, device) -> "GridBatch":
         device = _device(device)
         if device == self.device:

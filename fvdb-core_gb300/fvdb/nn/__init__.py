@@ -1,7 +1,30 @@
 """Neural-network layers of the sparse-convolution path."""
 
-from .modules import AvgPool, BatchNorm, GroupNorm, MaxPool, RecomputeSequential, ReLU, Sequential, SparseConv3d, UpsamplingNearest
+from .modules import (
+    CELU,
+    ELU,
+    GELU,
+    SELU,
+    AvgPool,
+    BatchNorm,
+    Dropout,
+    FillFromGrid,
+    GroupNorm,
+    LeakyReLU,
+    Linear,
+    MaxPool,
+    RecomputeSequential,
+    ReLU,
+    Sequential,
+    Sigmoid,
+    SiLU,
+    SparseConv3d,
+    SyncBatchNorm,
+    Tanh,
+    UpsamplingNearest,
+)
 from .vdbtensor import VDBTensor
 
-__all__ = ["SparseConv3d", "ReLU", "Sequential", "RecomputeSequential", "VDBTensor", "MaxPool", "AvgPool",
-           "UpsamplingNearest", "BatchNorm", "GroupNorm"]
+__all__ = ["VDBTensor", "MaxPool", "AvgPool", "UpsamplingNearest", "FillFromGrid", "SparseConv3d", "GroupNorm",
+           "BatchNorm", "SyncBatchNorm", "Linear", "ReLU", "LeakyReLU", "ELU", "CELU", "GELU", "SELU", "SiLU", "Tanh",
+           "Sigmoid", "Dropout", "Sequential", "RecomputeSequential"]

@@ -134,11 +134,58 @@ class SparseConv3d(nn.Module):
         return VDBTensor(out_grid, out_feature, out_kmap)
 
 
-class ReLU(nn.ReLU):
-    """Elementwise ReLU on a VDBTensor's features (grid and kernel map unchanged)."""
+class _OnFeatures:
+    """Runs the torch layer it is mixed into on a VDBTensor's [N, C] features; grid and kernel
+    map pass through (reference: fvdb/nn/modules.py:529-620)."""
 
     def forward(self, input: VDBTensor) -> VDBTensor:
+        if not isinstance(input, VDBTensor):
+            raise TypeError("Input should have type VDBTensor")
         return VDBTensor(input.grid, input.data.jagged_like(super().forward(input.data.jdata)), input.kmap)
+
+
+class ReLU(_OnFeatures, nn.ReLU):
+    """max(x, 0) on the features."""
+
+
+class LeakyReLU(_OnFeatures, nn.LeakyReLU):
+    """max(0, x) + negative_slope * min(0, x) on the features."""
+
+
+class ELU(_OnFeatures, nn.ELU):
+    """x for x > 0, alpha * (exp(x) - 1) otherwise, on the features."""
+
+
+class CELU(_OnFeatures, nn.CELU):
+    """max(0, x) + min(0, alpha * (exp(x / alpha) - 1)) on the features."""
+
+
+class GELU(_OnFeatures, nn.GELU):
+    """x * Phi(x) on the features."""
+
+
+class SELU(_OnFeatures, nn.SELU):
+    """scale * (max(0, x) + min(0, alpha * (exp(x) - 1))) on the features."""
+
+
+class SiLU(_OnFeatures, nn.SiLU):
+    """x * sigmoid(x) on the features."""
+
+
+class Tanh(_OnFeatures, nn.Tanh):
+    """tanh(x) on the features."""
+
+
+class Sigmoid(_OnFeatures, nn.Sigmoid):
+    """1 / (1 + exp(-x)) on the features."""
+
+
+class Linear(_OnFeatures, nn.Linear):
+    """x A^T + b on each voxel's feature row."""
+
+
+class Dropout(_OnFeatures, nn.Dropout):
+    """Bernoulli dropout of the features in training mode."""
 
 
 class BatchNorm(nn.BatchNorm1d):
@@ -162,6 +209,39 @@ class BatchNorm(nn.BatchNorm1d):
         if self.bias is not None:
             t = t + self.bias.detach().float()
         return s, t
+
+
+class SyncBatchNorm(nn.SyncBatchNorm):
+    """Batch normalisation of a VDBTensor's features with statistics over all ranks of the
+    process group (reference: fvdb/nn/modules.py:447-526): torch's SyncBatchNorm on the [N, C]
+    feature matrix."""
+
+    def forward(self, input: VDBTensor) -> VDBTensor:
+        if input.data.jdata.size(1) != self.num_features:
+            raise ValueError("Input feature should have the same number of channels as BatchNorm")
+        return VDBTensor(input.grid, input.grid.jagged_like(super().forward(input.data.jdata)), input.kmap)
+
+    @classmethod
+    def convert_sync_batchnorm(cls, module: nn.Module, process_group=None) -> nn.Module:
+        """A copy of `module` with every fvdb.nn.BatchNorm replaced by a SyncBatchNorm that holds
+        the same parameters, buffers and mode."""
+        out = module
+        if isinstance(module, BatchNorm):
+            out = cls(module.num_features, module.eps, module.momentum, module.affine, module.track_running_stats,
+                      process_group)
+            if module.affine:
+                with torch.no_grad():
+                    out.weight = module.weight
+                    out.bias = module.bias
+            out.running_mean = module.running_mean
+            out.running_var = module.running_var
+            out.num_batches_tracked = module.num_batches_tracked
+            out.train(module.training)
+            if hasattr(module, "qconfig"):
+                out.qconfig = module.qconfig
+        for name, child in module.named_children():
+            out.add_module(name, cls.convert_sync_batchnorm(child, process_group))
+        return out
 
 
 class GroupNorm(nn.GroupNorm):
@@ -287,6 +367,29 @@ class AvgPool(nn.Module):
 
     def extra_repr(self) -> str:
         return "kernel_size={kernel_size}, stride={stride}".format(kernel_size=self.kernel_size, stride=self.stride)
+
+
+class FillFromGrid(nn.Module):
+    """Moves a VDBTensor's features onto another grid: voxels the input's grid also holds take
+    its features, the rest `default_value` (reference: fvdb/nn/modules.py:132-154, through
+    GridBatch.inject_from).  Without a target the input is returned."""
+
+    def __init__(self, default_value: float = 0.0) -> None:
+        super().__init__()
+        self.default_value = default_value
+
+    def forward(self, input: VDBTensor, other_data: Optional[GridOrVDBTensor] = None) -> VDBTensor:
+        if isinstance(other_data, VDBTensor):
+            other_grid, other_kmap = other_data.grid, other_data.kmap
+        elif isinstance(other_data, GridBatch):
+            other_grid, other_kmap = other_data, None
+        else:
+            return input
+        feats = other_grid.inject_from(input.grid, input.data, default_value=self.default_value)
+        return VDBTensor(other_grid, feats, kmap=other_kmap)
+
+    def extra_repr(self) -> str:
+        return f"default_value={self.default_value}"
 
 
 class UpsamplingNearest(nn.Module):

@@ -1,0 +1,107 @@
+"""The feature-wise layers of fvdb.nn and FillFromGrid / GridBatch.inject_from.
+
+* Every activation, Linear and Dropout layer equals the torch layer on the [N, C] features, with
+  grid and kernel map passed through (reference: fvdb/nn/modules.py:529-620).
+* inject_from copies rows of the source grid's voxels that the destination holds, grid by grid in
+  index space, and fills the rest with default_value (or keeps dst): checked against a host
+  dictionary of (grid, i, j, k) -> row; gradients reach the injected rows only.
+* FillFromGrid is inject_from onto the other VDBTensor's grid, keeping its kernel map.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from tests.helpers import random_sparse_ijk
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(fvdb, dev, sizes, extent, seed):
+    parts = [torch.from_numpy(random_sparse_ijk(n, extent, seed + i)).to(dev) for i, n in enumerate(sizes)]
+    return fvdb.GridBatch.from_ijk(fvdb.JaggedTensor(parts))
+
+
+@pytest.mark.parametrize("name,args", [("ReLU", ()), ("LeakyReLU", (0.1,)), ("ELU", (0.7,)), ("CELU", (1.3,)),
+                                       ("GELU", ()), ("SELU", ()), ("SiLU", ()), ("Tanh", ()), ("Sigmoid", ()),
+                                       ("Linear", (16, 8)), ("Dropout", (0.3,))])
+def test_feature_layers_equal_torch(cuda_device, name, args):
+    import fvdb
+    import fvdb.nn as fvnn
+
+    grid = _batch(fvdb, cuda_device, [500, 900], 16, 5)
+    x = torch.randn(grid.total_voxels, 16, device=cuda_device)
+    kmap, _ = grid.sparse_conv_kernel_map(3, 1)
+    t = fvnn.VDBTensor(grid, grid.jagged_like(x), kmap)
+    ours = getattr(fvnn, name)(*args).to(cuda_device).eval()
+    ref = getattr(torch.nn, name)(*args).to(cuda_device).eval()
+    ref.load_state_dict(ours.state_dict())
+    out = ours(t)
+    assert out.grid.is_same(grid) and out.kmap is kmap
+    assert torch.equal(out.data.jdata, ref(x))
+    with pytest.raises(TypeError):
+        ours(x)
+
+
+def _rows(grid):
+    ijk = grid.ijk.jdata.cpu().numpy()
+    b = grid.jidx.cpu().numpy() if hasattr(grid, "jidx") else None
+    off = grid.joffsets.cpu().numpy()
+    bidx = np.repeat(np.arange(len(off) - 1), np.diff(off)) if b is None else b.astype(np.int64)
+    return {(int(bi), *map(int, c)): r for r, (bi, c) in enumerate(zip(bidx, ijk))}
+
+
+def test_inject_from_matches_host_lookup(cuda_device):
+    import fvdb
+
+    src = _batch(fvdb, cuda_device, [3000, 0, 1500], 20, 11)
+    dst = _batch(fvdb, cuda_device, [2500, 700, 1800], 20, 11 + 50)  # overlapping, not equal
+    g = torch.Generator().manual_seed(3)
+    x = torch.randn(src.total_voxels, 5, generator=g).to(cuda_device).requires_grad_(True)
+    out = dst.inject_from(src, src.jagged_like(x), default_value=-7.0)
+    srows = _rows(src)
+    expect = np.full((dst.total_voxels, 5), -7.0, np.float32)
+    xn = x.detach().cpu().numpy()
+    hit = []
+    for key, r in _rows(dst).items():
+        if key in srows:
+            expect[r] = xn[srows[key]]
+            hit.append(srows[key])
+    assert hit, "the grids should overlap"
+    assert np.array_equal(out.jdata.detach().cpu().numpy(), expect)
+    out.jdata.sum().backward()
+    gexp = np.zeros(src.total_voxels)
+    gexp[hit] = 1
+    assert np.array_equal(x.grad[:, 0].cpu().numpy(), gexp)
+    # into an existing destination: rows without a source voxel keep their values
+    d0 = torch.randn(dst.total_voxels, 5, generator=g).to(cuda_device)
+    out2 = dst.inject_from(src, src.jagged_like(x.detach()), dst.jagged_like(d0.clone()))
+    miss = torch.ones(dst.total_voxels, dtype=torch.bool)
+    for key, r in _rows(dst).items():
+        if key in srows:
+            miss[r] = False
+    miss = miss.to(cuda_device)
+    assert torch.equal(out2.jdata[miss], d0[miss])
+    assert torch.equal(out2.jdata[~miss], out.jdata.detach()[~miss])
+    with pytest.raises(ValueError):
+        dst.inject_from(src, src.jagged_like(x.detach()), dst.jagged_like(torch.zeros(dst.total_voxels, 4,
+                                                                                        device=cuda_device)))
+
+
+def test_fill_from_grid(cuda_device):
+    import fvdb
+    import fvdb.nn as fvnn
+
+    a = _batch(fvdb, cuda_device, [1200], 14, 21)
+    b = _batch(fvdb, cuda_device, [1500], 14, 22)
+    x = torch.randn(a.total_voxels, 3, device=cuda_device)
+    kb, _ = b.sparse_conv_kernel_map(3, 1)
+    other = fvnn.VDBTensor(b, b.jagged_like(torch.zeros(b.total_voxels, 3, device=cuda_device)), kb)
+    layer = fvnn.FillFromGrid(default_value=2.5)
+    out = layer(fvnn.VDBTensor(a, a.jagged_like(x)), other)
+    assert out.grid.is_same(b) and out.kmap is kb
+    assert torch.equal(out.data.jdata, b.inject_from(a, a.jagged_like(x), default_value=2.5).jdata)
+    out_g = layer(fvnn.VDBTensor(a, a.jagged_like(x)), b)
+    assert out_g.kmap is None and torch.equal(out_g.data.jdata, out.data.jdata)
+    same = fvnn.VDBTensor(a, a.jagged_like(x))
+    assert layer(same) is same

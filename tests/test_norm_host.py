@@ -36,3 +36,19 @@ def test_conv_folds_bias_into_shift():
     assert torch.allclose(shift, conv.bias.detach() * s + t)
     conv_nb = fvnn.SparseConv3d(4, 6, 3, bias=False)
     assert torch.equal(conv_nb._folded((s, t))[1], t)
+
+
+def test_convert_sync_batchnorm_keeps_state():
+    import fvdb.nn as fvnn
+
+    net = torch.nn.Sequential(fvnn.SparseConv3d(4, 8, 3), fvnn.BatchNorm(8), fvnn.ReLU(),
+                              torch.nn.Sequential(fvnn.BatchNorm(8, affine=False)))
+    with torch.no_grad():
+        net[1].running_mean.fill_(0.25)
+        net[1].weight.fill_(3.0)
+    net[3][0].eval()
+    out = fvnn.SyncBatchNorm.convert_sync_batchnorm(net)
+    assert type(out[1]) is fvnn.SyncBatchNorm and type(out[3][0]) is fvnn.SyncBatchNorm
+    assert out[1].weight is net[1].weight and torch.equal(out[1].running_mean, torch.full((8,), 0.25))
+    assert out[3][0].weight is None and not out[3][0].training
+    assert type(out[0]) is fvnn.SparseConv3d and type(out[2]) is fvnn.ReLU
