@@ -23,8 +23,8 @@ from .modules import (
     Tanh,
     UpsamplingNearest,
 )
-from .vdbtensor import VDBTensor
+from .vdbtensor import VDBTensor, vdbtensor_from_dense
 
-__all__ = ["VDBTensor", "MaxPool", "AvgPool", "UpsamplingNearest", "FillFromGrid", "SparseConv3d", "GroupNorm",
+__all__ = ["VDBTensor", "vdbtensor_from_dense", "MaxPool", "AvgPool", "UpsamplingNearest", "FillFromGrid", "SparseConv3d", "GroupNorm",
            "BatchNorm", "SyncBatchNorm", "Linear", "ReLU", "LeakyReLU", "ELU", "CELU", "GELU", "SELU", "SiLU", "Tanh",
            "Sigmoid", "Dropout", "Sequential", "RecomputeSequential"]

@@ -105,3 +105,40 @@ def test_fill_from_grid(cuda_device):
     assert out_g.kmap is None and torch.equal(out_g.data.jdata, out.data.jdata)
     same = fvnn.VDBTensor(a, a.jagged_like(x))
     assert layer(same) is same
+
+
+def test_vdbtensor_arithmetic_keeps_grid_and_map(cuda_device):
+    import fvdb
+    import fvdb.nn as fvnn
+
+    grid = _batch(fvdb, cuda_device, [600, 400], 12, 31)
+    kmap, _ = grid.sparse_conv_kernel_map(3, 1)
+    a0 = torch.rand(grid.total_voxels, 4, device=cuda_device) + 0.5
+    b0 = torch.rand(grid.total_voxels, 4, device=cuda_device) + 0.5
+    a = fvnn.VDBTensor(grid, grid.jagged_like(a0.clone()), kmap)
+    b = fvnn.VDBTensor(grid, grid.jagged_like(b0.clone()))
+    for got, want in [(a + b, a0 + b0), (a - b, a0 - b0), (a * b, a0 * b0), (a / b, a0 / b0), (a ** 2, a0 ** 2),
+                      (2.0 * a, 2.0 * a0), (-a, -a0), (a // b, a0 // b0), (a % b, a0 % b0), (a > b, a0 > b0),
+                      (a.sqrt(), a0.sqrt()), ((a - 1).abs(), (a0 - 1).abs()), (a.floor(), a0.floor())]:
+        assert got.grid.is_same(grid) and got.kmap is kmap
+        assert torch.equal(got.jdata, want)
+    c = a.clone()
+    c += b
+    c *= 3
+    assert torch.equal(c.jdata, (a0 + b0) * 3) and torch.equal(a.jdata, a0)
+    other = _batch(fvdb, cuda_device, [10], 12, 99)
+    with pytest.raises(ValueError):
+        a + fvnn.VDBTensor(other, other.jagged_like(torch.zeros(other.total_voxels, 4, device=cuda_device)))
+    g0 = a[1]
+    assert g0.grid.total_voxels == grid.num_voxels_at(1) and torch.equal(g0.jdata, a0[grid.cum_voxels_at(1):])
+    assert a.to(torch.float64).dtype == torch.float64 and a.detach().requires_grad is False
+
+
+def test_vdbtensor_from_dense_round_trip(cuda_device):
+    import fvdb.nn as fvnn
+
+    dense = torch.randn(2, 5, 6, 7, 3, device=cuda_device)
+    t = fvnn.vdbtensor_from_dense(dense, ijk_min=[-2, 1, 4])
+    assert t.grid_count == 2 and t.total_voxels == 2 * 5 * 6 * 7
+    assert torch.equal(t.grid.ijk.jdata.min(0).values.cpu(), torch.tensor([-2, 1, 4], dtype=torch.int32))
+    assert torch.equal(t.to_dense(), dense)
