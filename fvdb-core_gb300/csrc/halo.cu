@@ -341,14 +341,15 @@ template <typename T>
 int launch_halo_wgrad(const FvgbGrid &g, const void *x, int64_t ldx, int32_t Cin, const void *dy, int64_t lddy,
                       int32_t Cout, void *dw, void *ws, size_t ws_bytes, cudaStream_t s) {
     using A = typename HNum<T>::A;
-    const int tiles_ci = (int)ceil_div(Cin, 32), tiles_co = (int)ceil_div(Cout, 64);
-    const int64_t chunks = halo_chunks(g.num_leaves, tiles_ci * tiles_co);
+    const int64_t tiles_ci = ceil_div(Cin, 32), tiles_co = ceil_div(Cout, 64);
+    if (tiles_ci * tiles_co > 65535) return FVGB_EINVAL;  // one grid z slice per channel tile
+    const int64_t chunks = halo_chunks(g.num_leaves, (int)(tiles_ci * tiles_co));
     const int64_t per_chunk = 27LL * Cin * Cout;
     if (ws_bytes < (size_t)(chunks * per_chunk) * sizeof(A)) return FVGB_ENOSPACE;
     const int64_t lpc = ceil_div(std::max<int64_t>(g.num_leaves, 1), chunks);
     const dim3 grid((unsigned)chunks, 27, (unsigned)(tiles_ci * tiles_co));
-    halo_wgrad_kernel<T><<<grid, kHT, 0, s>>>(g, (const T *)x, ldx, Cin, (const T *)dy, lddy, Cout, lpc, tiles_co,
-                                             (A *)ws);
+    halo_wgrad_kernel<T><<<grid, kHT, 0, s>>>(g, (const T *)x, ldx, Cin, (const T *)dy, lddy, Cout, lpc,
+                                             (int)tiles_co, (A *)ws);
     halo_wgrad_reduce_kernel<A, T><<<(unsigned)ceil_div(per_chunk, 256), 256, 0, s>>>((const A *)ws, chunks, per_chunk,
                                                                                      (T *)dw);
     count_launches(2);
@@ -379,6 +380,7 @@ extern "C" int fvgb_halo_conv(int32_t dtype, const FvgbGrid *grid, const void *x
 extern "C" int fvgb_halo_wgrad_workspace(int32_t dtype, const FvgbGrid *grid, int32_t c_in, int32_t c_out,
                                          size_t *bytes) {
     if (!grid || !bytes || c_in < 1 || c_out < 1) return FVGB_EINVAL;
+    if (ceil_div(c_in, 32) * ceil_div(c_out, 64) > 65535) return FVGB_EINVAL;
     const int tiles = (int)(ceil_div(c_in, 32) * ceil_div(c_out, 64));
     const size_t elem = dtype == FVGB_F64 ? 8 : 4;
     *bytes = (size_t)halo_chunks(grid->num_leaves, tiles) * 27 * c_in * c_out * elem + 256;
