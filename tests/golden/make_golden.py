@@ -112,6 +112,35 @@ def transposed_case(name, extent, cin, cout, k, seed):
     print(name, g.shape[0])
 
 
+def transposed_strided_case(name, n, extent, cin, cout, ks, st, seed, lo=0, shift=12):
+    """Strided transposed conv (the decoder side of a UNet: coarse features onto the fine grid
+    whose forward map defines the pairs).  Features live on the coarse target set of
+    (ijk, ks, st); the expected output on the fine voxels is torch's dense conv_transpose3d, the
+    adjoint of the dense conv3d whose restriction the sparse forward is."""
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(extent**3, size=n, replace=False)
+    ijk = (np.stack([idx // extent**2, (idx // extent) % extent, idx % extent], 1) + lo).astype(np.int32)
+    tgt = np.array(target_set(ijk, ks, st), dtype=np.int64).reshape(-1, 3)
+    x = rng.standard_normal((tgt.shape[0], cin))
+    w = rng.standard_normal((cin, cout) + tuple(ks)) / math.sqrt(cin * np.prod(ks))
+    sax = [st[2], st[1], st[0]]
+    kax = [ks[2], ks[1], ks[0]]
+    osz = [int(tgt[:, a].max()) + shift // sax[a] + 2 + kax[a] for a in range(3)]
+    d = torch.zeros(osz + [cin], dtype=torch.float64)
+    d[tuple(torch.from_numpy(tgt[:, a] + shift // sax[a]) for a in range(3))] = torch.from_numpy(x)
+    pad = [-kstart(k) for k in ks]
+    y = torch.nn.functional.conv_transpose3d(d.permute(3, 2, 1, 0)[None], torch.from_numpy(w), stride=tuple(st),
+                                             padding=pad)[0]
+    fi = [torch.from_numpy(ijk[:, a].astype(np.int64) + shift) for a in range(3)]
+    assert all(int(fi[a].max()) < y.shape[3 - a] for a in range(3))
+    expected = y[:, fi[2], fi[1], fi[0]].T.numpy()
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"), ijk=ijk, features=x, weights=w, kernel_size=np.array(ks),
+        stride=np.array(st), target_ijk=tgt.astype(np.int32), expected=expected,
+    )
+    print(name, ijk.shape[0], "<-", tgt.shape[0])
+
+
 if __name__ == "__main__":
     case("sparse_k3_s1_c16", 2000, 24, 16, 16, (3, 3, 3), (1, 1, 1), seed=0)
     case("sparse_k3_s2_c8", 1500, 20, 8, 12, (3, 3, 3), (2, 2, 2), seed=1)
@@ -120,3 +149,9 @@ if __name__ == "__main__":
     case("sparse_k5_s2_neg", 600, 14, 4, 4, (5, 5, 5), (2, 2, 2), seed=4, lo=-6)
     transposed_case("dense_transposed_k3", 8, 4, 8, 3, seed=5)
     transposed_case("dense_transposed_k4", 8, 4, 8, 4, seed=6)
+    case("sparse_k2_s1_c8", 1500, 18, 8, 8, (2, 2, 2), (1, 1, 1), seed=7)
+    case("sparse_k4_s2_c4", 900, 16, 4, 6, (4, 4, 4), (2, 2, 2), seed=8, lo=-5)
+    case("sparse_k3_s3_c4", 1200, 18, 4, 4, (3, 3, 3), (3, 3, 3), seed=9, lo=-4)
+    transposed_strided_case("strided_transposed_k2_s2", 1200, 16, 8, 4, (2, 2, 2), (2, 2, 2), seed=10, lo=-3)
+    transposed_strided_case("strided_transposed_k3_s2", 900, 14, 4, 6, (3, 3, 3), (2, 2, 2), seed=11)
+    transposed_strided_case("strided_transposed_aniso", 700, 14, 4, 4, (3, 2, 1), (1, 2, 3), seed=12, lo=-2)

@@ -34,3 +34,18 @@ def test_oracle_transposed_matches_golden(name):
     perm = [rows_by_coord(g["ijk"])[tuple(r)] for r in src.tolist()]
     out = orc.conv_forward_f64(g["features"][perm], g["weights"], kmap, transposed=True, n_src=src.shape[0])
     np.testing.assert_allclose(out, g["expected"][perm], rtol=1e-10, atol=1e-10)
+
+
+@pytest.mark.parametrize("name", golden_cases("strided_transposed"))
+def test_oracle_strided_transposed_matches_golden(name):
+    """Coarse features onto the fine grid through the fine -> coarse forward map."""
+    g = load_golden(name)
+    ks, st = tuple(g["kernel_size"].tolist()), tuple(g["stride"].tolist())
+    src, soff = orc.grid_from_ijk(g["ijk"], np.array([0, g["ijk"].shape[0]]))
+    tgt, toff = orc.conv_grid(src, soff, ks, st)
+    assert set(map(tuple, tgt.tolist())) == set(map(tuple, g["target_ijk"].tolist()))
+    kmap = orc.kernel_map(src, soff, tgt, toff, ks, st)
+    xt = g["features"][[rows_by_coord(g["target_ijk"])[tuple(r)] for r in tgt.tolist()]]
+    out = orc.conv_forward_f64(xt, g["weights"], kmap, transposed=True, n_src=src.shape[0])
+    perm = [rows_by_coord(g["ijk"])[tuple(r)] for r in src.tolist()]
+    np.testing.assert_allclose(out, g["expected"][perm], rtol=1e-10, atol=1e-10)

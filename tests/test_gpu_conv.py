@@ -82,6 +82,25 @@ def test_golden_transposed(fvdb, cuda_device, name):
     assert rel_max(out, g["expected"][perm]) < 1e-12
 
 
+@pytest.mark.parametrize("name", golden_cases("strided_transposed"))
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_golden_strided_transposed(fvdb, cuda_device, name, dtype):
+    """Coarse features onto the fine grid (sparse_transpose_conv_3d over the fine -> coarse map)
+    against torch's dense conv_transpose3d."""
+    g = load_golden(name)
+    ks, st = tuple(g["kernel_size"].tolist()), tuple(g["stride"].tolist())
+    grid = fvdb.GridBatch.from_ijk(torch.from_numpy(g["ijk"]).to(cuda_device))
+    pack, tgt = grid.sparse_conv_kernel_map(ks, st)
+    t_rows = rows_by_coord(g["target_ijk"])
+    xt = g["features"][[t_rows[tuple(r)] for r in tgt.ijk.jdata.cpu().numpy().tolist()]]
+    x = torch.from_numpy(xt).to(cuda_device, dtype)
+    w = torch.from_numpy(g["weights"]).to(cuda_device, dtype)
+    out = pack.sparse_transpose_conv_3d(x, w).jdata.double().cpu().numpy()
+    perm = [rows_by_coord(g["ijk"])[tuple(r)] for r in grid.ijk.jdata.cpu().numpy().tolist()]
+    tol = 1e-12 if dtype == torch.float64 else 1e-5
+    assert rel_max(out, g["expected"][perm]) < tol
+
+
 CASES = [((3, 3, 3), (1, 1, 1), 16, 32), ((2, 2, 2), (2, 2, 2), 32, 16), ((3, 3, 3), (2, 2, 2), 8, 24),
          ((5, 3, 1), (1, 3, 2), 4, 8), ((3, 3, 3), (1, 1, 1), 70, 130)]
 
