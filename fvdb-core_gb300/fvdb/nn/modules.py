@@ -287,8 +287,11 @@ class Sequential(nn.Sequential):
         while i < len(mods):
             m = mods[i]
             nxt = mods[i + 1] if i + 1 < len(mods) else None
+            # folded only where the layers' own output dtype is the features' (a bias of a wider
+            # dtype would promote the unfused result)
             if (isinstance(m, SparseConv3d) and type(nxt) is BatchNorm and not torch.is_grad_enabled()
-                    and m.precision == "native"):
+                    and m.precision == "native" and isinstance(input, VDBTensor)
+                    and (m.bias is None or m.bias.dtype == input.data.jdata.dtype)):
                 aff = nxt.folded_affine()
                 if aff is not None and aff[0].device == m.weight.device:
                     after = mods[i + 2] if i + 2 < len(mods) else None

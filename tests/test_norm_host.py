@@ -52,3 +52,29 @@ def test_convert_sync_batchnorm_keeps_state():
     assert out[1].weight is net[1].weight and torch.equal(out[1].running_mean, torch.full((8,), 0.25))
     assert out[3][0].weight is None and not out[3][0].training
     assert type(out[0]) is fvnn.SparseConv3d and type(out[2]) is fvnn.ReLU
+
+
+def test_sequential_does_not_fold_across_dtype_promotion(monkeypatch):
+    """A wider bias than the features would promote the unfused output, so the fold is skipped."""
+    import fvdb.nn as fvnn
+    from fvdb.nn import modules
+
+    conv, bn = fvnn.SparseConv3d(4, 6, 3), fvnn.BatchNorm(6).eval()
+    seq = fvnn.Sequential(conv, bn)
+    calls = []
+    monkeypatch.setattr(modules.SparseConv3d, "forward", lambda self, x, **k: calls.append(k) or x)
+    monkeypatch.setattr(modules.BatchNorm, "forward", lambda self, x: x)
+
+    class Feats:
+        jdata = torch.zeros(3, 4, dtype=torch.bfloat16)
+
+    x = object.__new__(fvnn.VDBTensor)
+    x.data = Feats()
+    with torch.no_grad():
+        seq(x)
+    assert calls == [{}]  # conv bias is FP32, features BF16: layers run one by one
+    calls.clear()
+    Feats.jdata = torch.zeros(3, 4)
+    with torch.no_grad():
+        seq(x)
+    assert len(calls) == 1 and "out_affine" in calls[0]
