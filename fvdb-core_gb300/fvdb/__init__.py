@@ -6,7 +6,7 @@ SparseConvPackInfo, ConvPackBackend and fvdb.nn.{SparseConv3d, VDBTensor}.
 
 from . import _lib
 from .grid_batch import GridBatch
-from .jagged_tensor import JaggedTensor
+from .jagged_tensor import JaggedTensor, jcat
 from .sparse_conv_pack_info import ConvPackBackend, SparseConvPackInfo
 
 _lib.load()
@@ -14,4 +14,4 @@ _lib.load()
 from . import nn  # noqa: E402
 
 __version__ = "0.1.0"
-__all__ = ["GridBatch", "JaggedTensor", "SparseConvPackInfo", "ConvPackBackend", "nn"]
+__all__ = ["GridBatch", "JaggedTensor", "jcat", "SparseConvPackInfo", "ConvPackBackend", "nn"]

@@ -142,3 +142,28 @@ def test_vdbtensor_from_dense_round_trip(cuda_device):
     assert t.grid_count == 2 and t.total_voxels == 2 * 5 * 6 * 7
     assert torch.equal(t.grid.ijk.jdata.min(0).values.cpu(), torch.tensor([-2, 1, 4], dtype=torch.int32))
     assert torch.equal(t.to_dense(), dense)
+
+
+def test_jcat_grids_and_vdbtensors(cuda_device):
+    import fvdb
+    import fvdb.nn as fvnn
+
+    a = _batch(fvdb, cuda_device, [300, 500], 12, 41)
+    b = _batch(fvdb, cuda_device, [700], 12, 43)
+    ab = fvdb.jcat([a, b])
+    assert ab.grid_count == 3 and ab.total_voxels == a.total_voxels + b.total_voxels
+    assert torch.equal(ab.ijk.jdata, torch.cat([a.ijk.jdata, b.ijk.jdata]))
+    xa = torch.randn(a.total_voxels, 4, device=cuda_device)
+    xb = torch.randn(b.total_voxels, 4, device=cuda_device)
+    t = fvdb.jcat([fvnn.VDBTensor(a, a.jagged_like(xa)), fvnn.VDBTensor(b, b.jagged_like(xb))])
+    assert t.grid.grid_count == 3 and torch.equal(t.jdata, torch.cat([xa, xb]))
+    kmap, _ = a.sparse_conv_kernel_map(3, 1)
+    skip = fvnn.VDBTensor(a, a.jagged_like(xa), kmap)
+    up = fvnn.VDBTensor(a, a.jagged_like(xa * 2))
+    cat = fvdb.jcat([up, skip], dim=1)
+    assert cat.grid.is_same(a) and cat.jdata.shape == (a.total_voxels, 8)
+    assert torch.equal(cat.jdata, torch.cat([xa * 2, xa], 1))
+    with pytest.raises(ValueError):
+        fvdb.jcat([up, skip], dim=0)
+    with pytest.raises(ValueError):
+        fvdb.jcat([a, b], dim=1)
