@@ -250,7 +250,9 @@ class GroupNorm(nn.GroupNorm):
     over its voxels and the group's channels, with the biased variance and eps of
     torch.nn.GroupNorm.  One vectorised pass over all grids: the per-(grid, group) sums are
     segment sums keyed by the voxels' grid index, the variance is taken about the mean (two
-    passes, FP32 or wider), and empty grids contribute nothing."""
+    passes, FP32 or wider), and empty grids contribute nothing.  The segment sums accumulate with
+    atomics on CUDA, so results agree with the per-grid loop to rounding but are not bitwise
+    reproducible from run to run."""
 
     def forward(self, input: VDBTensor) -> VDBTensor:
         x = input.data.jdata
